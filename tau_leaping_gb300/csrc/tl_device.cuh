@@ -1,0 +1,905 @@
+// tl_device.cuh - device building blocks of the tau-leaping engine.
+//
+// Everything a realization does in one step lives here, written once and
+// instantiated for three cooperation widths (the "group" owning one
+// realization): one thread (G1), one warp (GWarp) or one CTA (GCta).  The
+// fused persistent kernel loops do_step() until a realization reaches
+// t_final; the plain form calls it once per launch.
+//
+// Reference semantics followed (CSSL-UWM/tau_leaping):
+//   propensity / criticality  tau_leaping/functions.h:100-123, model.cu:180-209
+//   CGP tau bound             tau_leaping/CSRMatrixPacked.cu:294-358
+//   leap / SSA branch         tau_leaping/model.cu:301-413
+//   critical channel draw     tau_leaping/model.cu:555-598
+//   Poisson firing            tau_leaping/model.cu:458-521
+//   integer state update      tau_leaping/CSRMatrixPacked.cu:464-503
+//   direct-method step        tau_leaping/model.cu:427-451
+// with the Cao-Gillespie-Petzold (J. Chem. Phys. 124, 044109, 2006) rules the
+// reference departs from switched by TL_FLAG_COMPAT_* bits.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/tl.h"
+
+namespace tl {
+
+#define TL_HD __host__ __device__ __forceinline__
+#define TL_D __device__ __forceinline__
+
+constexpr uint32_t kScalarChannel = 0xFFFFFFFFu;  // counter word 0 of step scalars
+constexpr float kInfF = __builtin_huge_valf();
+
+// Error bits written to the run's error word.
+enum : unsigned {
+    kErrOverflow = 1u << 0,
+    kErrWaitTimeout = 1u << 1,
+    kErrHalving = 1u << 2,    // leap halved 64 times without success
+    kErrNumeric = 1u << 3,
+    kErrStage = 1u << 4,
+};
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy
+// as 1, 2, 3", SC'11).  Round: (c0,c1,c2,c3) -> (hi(B*c2)^c1^k0, lo(B*c2),
+// hi(A*c0)^c3^k1, lo(A*c0)) with A=0xD2511F53, B=0xCD9E8D57; the key is
+// bumped by the Weyl constants between rounds.
+// ---------------------------------------------------------------------------
+struct U4 {
+    uint32_t x, y, z, w;
+};
+
+TL_HD uint32_t mulhi32(uint32_t a, uint32_t b) {
+#ifdef __CUDA_ARCH__
+    return __umulhi(a, b);
+#else
+    return (uint32_t)(((uint64_t)a * (uint64_t)b) >> 32);
+#endif
+}
+
+TL_HD U4 philox10(U4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        const uint32_t hi0 = mulhi32(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        const uint32_t hi1 = mulhi32(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    }
+    return c;
+}
+
+// Uniform in (0,1): 23 random bits at odd multiples of 2^-24 (exact in FP32).
+TL_HD float u01f(uint32_t w) { return ((float)(w >> 9) + 0.5f) * 1.1920928955078125e-07f; }
+// Uniform in (0,1) with 52 random bits, exact in FP64.
+TL_HD double u01d(uint32_t hi, uint32_t lo) {
+    const uint64_t k = ((uint64_t)(hi >> 6) << 26) | (uint64_t)(lo >> 6);
+    return ((double)k + 0.5) * 2.220446049250313e-16;
+}
+
+// Step scalars of (realization r, set s, step): 4 words.
+TL_HD U4 step_words(uint32_t k0, uint32_t k1, uint32_t step, uint32_t r, uint32_t set) {
+    return philox10(U4{kScalarChannel, step, r, set << 8}, k0, k1);
+}
+
+// Per-channel uniform stream: blocks (j, step, r, set<<8 | b), b = 0, 1, ...
+struct ChanRng {
+    U4 buf;
+    uint32_t j, step, r, c3, k0, k1;
+    int left;
+    TL_D void init(uint32_t j_, uint32_t step_, uint32_t r_, uint32_t set, uint32_t k0_, uint32_t k1_) {
+        j = j_;
+        step = step_;
+        r = r_;
+        c3 = set << 8;
+        k0 = k0_;
+        k1 = k1_;
+        left = 0;
+    }
+    TL_D float next() {
+        if (left == 0) {
+            buf = philox10(U4{j, step, r, c3}, k0, k1);
+            c3 += 1;  // next block; 256 blocks per (j, step) before wrapping into set+1
+            left = 4;
+        }
+        const uint32_t w = buf.x;
+        buf.x = buf.y;
+        buf.y = buf.z;
+        buf.z = buf.w;
+        --left;
+        return u01f(w);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Poisson samplers (FP32).
+// ---------------------------------------------------------------------------
+__device__ __constant__ const float kLogFact[10] = {
+    0.0f, 0.0f, 0.693147180559945f, 1.7917594692280554f, 3.178053830347945f,
+    4.787491742782047f, 6.579251212010102f, 8.525161361065415f, 10.604602902745249f,
+    12.801827480081467f};
+
+// log P(K = k) for K ~ Poisson(mu), mu >= 10, written so that FP32 keeps its
+// accuracy for large mu: with d = k - mu, r = d/mu and Stirling's series for
+// log k!,  log p = -(k*(log1p(r) - r) + d*r) - 0.5*log(2*pi*k) - delta(k),
+// delta(k) = 1/(12k) - 1/(360k^3) + 1/(1260k^5).
+TL_D float log_poisson_pmf(float kf, float mu, float lmu) {
+    if (kf < 10.f) return kf * lmu - mu - kLogFact[(int)kf];
+    const float d = kf - mu;
+    const float r = d / mu;
+    float l1mr;  // log1p(r) - r
+    if (fabsf(r) <= 0.01f) {
+        // -r^2/2 + r^3/3 - r^4/4 + r^5/5 - r^6/6
+        l1mr = r * r * (-0.5f + r * (1.f / 3.f + r * (-0.25f + r * (0.2f - r * (1.f / 6.f)))));
+    } else {
+        l1mr = log1pf(r) - r;
+    }
+    const float t = kf * l1mr + d * r;
+    const float ik = 1.f / kf, ik2 = ik * ik;
+    const float delta = ik * (1.f / 12.f - ik2 * (1.f / 360.f - ik2 * (1.f / 1260.f)));
+    return -t - 0.5f * logf(6.283185307179586f * kf) - delta;
+}
+
+// Hormann's PTRS transformed rejection (Insurance: Mathematics and Economics
+// 12, 39-45, 1993), valid for mu >= 10.
+template <class Rng>
+TL_D int poisson_ptrs(float mu, Rng& rng) {
+    const float smu = sqrtf(mu);
+    const float lmu = logf(mu);
+    const float b = 0.931f + 2.53f * smu;
+    const float a = -0.059f + 0.02483f * b;
+    const float inv_alpha = 1.1239f + 1.1328f / (b - 3.4f);
+    const float vr = 0.9277f - 3.6224f / (b - 2.f);
+    for (int it = 0; it < 512; ++it) {
+        const float U = rng.next() - 0.5f;
+        const float V = rng.next();
+        const float us = 0.5f - fabsf(U);
+        const float kf = floorf((2.f * a / us + b) * U + mu + 0.43f);
+        if (us >= 0.07f && V <= vr) return (int)kf;
+        if (kf < 0.f || (us < 0.013f && V > us)) continue;
+        const float lhs = logf(V * inv_alpha / (a / (us * us) + b));
+        if (lhs <= log_poisson_pmf(kf, mu, lmu)) return (int)kf;
+    }
+    return (int)(mu + 0.5f);  // unreachable in practice (acceptance > 0.89)
+}
+
+// Sequential-search inversion for mu < 10 with one uniform per attempt.  If
+// the FP32 CDF stops growing before it passes u (u above the representable
+// mass) the uniform is discarded and a fresh one drawn, so no tail value is
+// ever produced by rounding.
+template <class Rng>
+TL_D int poisson_inversion(float mu, Rng& rng) {
+    const float emu = expf(-mu);
+    for (int attempt = 0; attempt < 16; ++attempt) {
+        const float u = rng.next();
+        float p = emu, F = emu;
+        int k = 0;
+        bool ok = true;
+        while (u > F) {
+            ++k;
+            p = p * __fdividef(mu, (float)k);
+            const float Fn = F + p;
+            if (Fn == F) {
+                ok = false;
+                break;
+            }
+            F = Fn;
+        }
+        if (ok) return k;
+    }
+    return (int)mu;
+}
+
+template <class Rng>
+TL_D int poisson_cgp(float mu, Rng& rng) {
+    if (!(mu > 0.f)) return 0;
+    if (mu < 10.f) return poisson_inversion(mu, rng);
+    return poisson_ptrs(mu, rng);
+}
+
+// The reference's sampler (model.cu:477-520, functions.h:37-54): Knuth's
+// product method below mean 80 capped at 300 firings, |Normal(mean, mean)|
+// from the polar Box-Muller draw above, truncated toward zero.
+template <class Rng>
+TL_D int poisson_reference(float mu, Rng& rng) {
+    if (mu < 80.f) {
+        const float lam = 1.f / expf(mu);
+        float val = 1.f;
+        for (int n = 1; n < 300; ++n) {
+            val *= rng.next();
+            if (val < lam) return n - 1;
+        }
+        return 300;
+    }
+    float u, v, s;
+    int it = 0;
+    do {
+        u = 2.f * rng.next() - 1.f;
+        v = 2.f * rng.next() - 1.f;
+        s = u * u + v * v;
+    } while (s >= 1.f && ++it < 64);
+    const float z = u * sqrtf(-2.f * logf(s) / s);
+    return (int)fabsf(mu + sqrtf(mu) * z);
+}
+
+// ---------------------------------------------------------------------------
+// Propensity and criticality of one channel (functions.h:100-123).
+// chan = {s0, s1, order, reference order}; order 0 = no reactant (a = c).
+// ---------------------------------------------------------------------------
+template <class Pop>
+TL_D void propensity(const int4 ch, float c, const Pop* x, int nc, bool compat_crit, float& a,
+                     bool& crit) {
+    const int order = ch.z;
+    if (order == 1) {
+        const Pop x0 = x[ch.x];
+        a = c * (float)x0;
+        crit = x0 < (Pop)nc;
+    } else if (order == 2) {
+        const Pop x0 = x[ch.x], x1 = x[ch.y];
+        a = c * (float)x0 * (float)x1;
+        crit = x0 < (Pop)nc || x1 < (Pop)nc;
+    } else if (order == 3) {
+        const Pop x0 = x[ch.x];
+        a = c * (float)x0 * (float)(x0 - 1) * 0.5f;
+        crit = compat_crit ? (x0 * 2 < (Pop)nc) : (x0 < (Pop)(2 * nc));
+    } else {
+        a = c;
+        crit = false;
+    }
+}
+
+// g_i of the CGP bound.  kind: 0 not a reactant, 1 HOR 1, 2 HOR 2 (S_i+S_k),
+// 3 HOR 2 with 2S_i (g = 2 + 1/(x-1)).  The reference's GetG
+// (CSRMatrixPacked.cu:294-309) maps channel orders 1,2,3 the same way.
+TL_D float g_of(int kind, float x) {
+    if (kind == 1) return 1.f;
+    if (kind == 2) return 2.f;
+    if (kind == 3) return x >= 2.f ? 2.f + 1.f / (x - 1.f) : 3.f;
+    return 0.f;
+}
+
+TL_D bool is_crit(float a) { return __float_as_uint(a) >> 31; }
+
+// ---------------------------------------------------------------------------
+// Groups: the threads that own one realization.
+// ---------------------------------------------------------------------------
+struct G1 {
+    static constexpr int kWidth = 1;
+    TL_D int rank() const { return 0; }
+    TL_D int size() const { return 1; }
+    TL_D void sync() const {}
+    TL_D bool leader() const { return true; }
+    TL_D float sumf(float v) const { return v; }
+    TL_D double sumd(double v) const { return v; }
+    TL_D float minf(float v) const { return v; }
+    TL_D bool any(bool p) const { return p; }
+    TL_D double excl_scan(double) const { return 0.0; }
+    TL_D int first(bool p) const { return p ? 0 : -1; }
+    TL_D int last(bool p) const { return p ? 0 : -1; }
+    template <class T>
+    TL_D T bcast(T v, int) const {
+        return v;
+    }
+};
+
+struct GWarp {
+    static constexpr int kWidth = 32;
+    int lane;
+    TL_D int rank() const { return lane; }
+    TL_D int size() const { return 32; }
+    TL_D void sync() const { __syncwarp(); }
+    TL_D bool leader() const { return lane == 0; }
+    TL_D float sumf(float v) const {
+#pragma unroll
+        for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        return v;
+    }
+    TL_D double sumd(double v) const {
+#pragma unroll
+        for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        return v;
+    }
+    TL_D float minf(float v) const {
+#pragma unroll
+        for (int o = 16; o; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        return v;
+    }
+    TL_D bool any(bool p) const { return __any_sync(0xffffffffu, p); }
+    TL_D double excl_scan(double v) const {
+        double s = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double n = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += n;
+        }
+        const double e = __shfl_up_sync(0xffffffffu, s, 1);
+        return lane ? e : 0.0;
+    }
+    TL_D int first(bool p) const {
+        const unsigned b = __ballot_sync(0xffffffffu, p);
+        return b ? __ffs(b) - 1 : -1;
+    }
+    TL_D int last(bool p) const {
+        const unsigned b = __ballot_sync(0xffffffffu, p);
+        return b ? 31 - __clz(b) : -1;
+    }
+    template <class T>
+    TL_D T bcast(T v, int src) const {
+        return __shfl_sync(0xffffffffu, v, src);
+    }
+};
+
+// Whole CTA; needs a shared scratch of 34 doubles.  Every member is a
+// CTA-wide collective (call from all threads, uniform control flow).
+struct GCta {
+    static constexpr int kWidth = 0;
+    int tid, n, lane, warp, nwarps;
+    double* red;
+    TL_D int rank() const { return tid; }
+    TL_D int size() const { return n; }
+    TL_D void sync() const { __syncthreads(); }
+    TL_D bool leader() const { return tid == 0; }
+    TL_D float sumf(float v) const { return reduce_sum<float>(v); }
+    template <class T>
+    TL_D T reduce_sum(T v) const {
+#pragma unroll
+        for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        __syncthreads();
+        if (lane == 0) red[warp] = (double)v;
+        __syncthreads();
+        if (warp == 0) {
+            T x = lane < nwarps ? (T)red[lane] : (T)0;
+#pragma unroll
+            for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if (lane == 0) red[33] = (double)x;
+        }
+        __syncthreads();
+        return (T)red[33];
+    }
+    TL_D double sumd(double v) const { return reduce_sum<double>(v); }
+    TL_D float minf(float v) const {
+#pragma unroll
+        for (int o = 16; o; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        __syncthreads();
+        if (lane == 0) red[warp] = (double)v;
+        __syncthreads();
+        if (warp == 0) {
+            float x = lane < nwarps ? (float)red[lane] : kInfF;
+#pragma unroll
+            for (int o = 16; o; o >>= 1) x = fminf(x, __shfl_xor_sync(0xffffffffu, x, o));
+            if (lane == 0) red[33] = (double)x;
+        }
+        __syncthreads();
+        return (float)red[33];
+    }
+    TL_D bool any(bool p) const { return __syncthreads_or(p ? 1 : 0) != 0; }
+    TL_D double excl_scan(double v) const {
+        double s = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double t = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += t;
+        }
+        const double e_in = __shfl_up_sync(0xffffffffu, s, 1);
+        __syncthreads();
+        if (lane == 31) red[warp] = s;
+        __syncthreads();
+        if (warp == 0) {
+            double y = lane < nwarps ? red[lane] : 0.0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const double t = __shfl_up_sync(0xffffffffu, y, o);
+                if (lane >= o) y += t;
+            }
+            const double ex = __shfl_up_sync(0xffffffffu, y, 1);
+            if (lane < nwarps) red[lane] = lane ? ex : 0.0;  // exclusive warp offsets
+        }
+        __syncthreads();
+        const double off = red[warp];
+        __syncthreads();
+        return (lane ? e_in : 0.0) + off;
+    }
+    TL_D int first(bool p) const {
+        const unsigned b = __ballot_sync(0xffffffffu, p);
+        __syncthreads();
+        if (lane == 0) red[warp] = b ? (double)(warp * 32 + __ffs(b) - 1) : 1e9;
+        __syncthreads();
+        if (warp == 0) {
+            double x = lane < nwarps ? red[lane] : 1e9;
+#pragma unroll
+            for (int o = 16; o; o >>= 1) x = fmin(x, __shfl_xor_sync(0xffffffffu, x, o));
+            if (lane == 0) red[33] = x;
+        }
+        __syncthreads();
+        const double r = red[33];
+        return r > 1e8 ? -1 : (int)r;
+    }
+    TL_D int last(bool p) const {
+        const unsigned b = __ballot_sync(0xffffffffu, p);
+        __syncthreads();
+        if (lane == 0) red[warp] = b ? (double)(warp * 32 + 31 - __clz(b)) : -1.0;
+        __syncthreads();
+        if (warp == 0) {
+            double x = lane < nwarps ? red[lane] : -1.0;
+#pragma unroll
+            for (int o = 16; o; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+            if (lane == 0) red[33] = x;
+        }
+        __syncthreads();
+        return (int)red[33];
+    }
+    template <class T>
+    TL_D T bcast(T v, int src) const {
+        __syncthreads();
+        if (tid == src) red[32] = (double)v;
+        __syncthreads();
+        const T r = (T)red[32];
+        __syncthreads();
+        return r;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Model view (global or staged copy in shared memory).
+// ---------------------------------------------------------------------------
+struct MView {
+    const int4* chan;         // [M] {s0, s1, order, reference order}
+    const signed char* gkind; // [N]
+    const int* rp;            // [N+1] CSR used for mu/sigma^2
+    const int* vc;            // [nnz] packed (col<<3)|((v+2)&7)
+    const int* urp;           // [N+1] CSR used for the update (net entries)
+    const int* uvc;
+    const int* cp;            // [M+1] CSC net (direct-method firing)
+    const int* rv;            // [nnz] packed (row<<3)|((v+2)&7)
+};
+
+TL_HD int unpack_idx(int p) { return p >> 3; }
+TL_HD int unpack_v(int p) { return (p & 7) - 2; }
+
+struct SimParams {
+    int N, M;
+    MView g;            // global view
+    const void* x0;     // Pop[N]
+    const float* rates; // [S][M]
+    const double* t_final; // [S]
+    long long R;        // realizations per set in this call
+    long long r_off;    // id of the first realization (sharding)
+    int S;
+    uint32_t k0, k1;    // Philox key (seed)
+    float eps;
+    int nc;
+    float ssa_factor;
+    int ssa_block;
+    int n_int;          // grid intervals (points = n_int + 1)
+    int K;
+    const int* tracked; // [K]
+    void* samples;      // Pop[S*R][n_int+1][K]
+    float* scores;      // [S*R][M] when sensitivity is on
+    long long max_steps;
+    unsigned flags;
+    // staging of the constant blob into shared memory
+    const unsigned char* blob;
+    int stage_bytes;    // 0 = no staging
+    int off_chan, off_gkind, off_rp, off_vc, off_cp, off_rv;  // byte offsets (net)
+    int slot_bytes;     // per group
+    unsigned long long* ctr; // [0] work, [1] leaps, [2] ssa, [3] rejections,
+                             // [4] truncated, [5] error bits, [6] done count
+    // plain form state
+    void* pstate;
+    void* pslots;       // global slots for the plain form
+};
+
+template <class Pop>
+struct Slot {
+    Pop* x;
+    Pop* xn;
+    float* a;  // propensity (sign bit = critical); holds int firing counts after the Poisson pass
+};
+
+template <class TimeT>
+struct RState {
+    TimeT t;
+    int kpt;           // next grid point to record
+    uint32_t step;     // Philox step counter
+    int done;
+    long long nsteps;  // accepted steps (cap)
+    long long leaps, ssa, rej;
+};
+
+TL_HD bool flag(unsigned f, unsigned b) { return (f & b) != 0; }
+
+template <class TimeT>
+TL_D TimeT grid_time(const SimParams& p, double T, int k) {
+    if (k >= p.n_int) return (TimeT)T;
+    return (TimeT)(T * (double)k / (double)p.n_int);
+}
+
+// ---------------------------------------------------------------------------
+// Passes.
+// ---------------------------------------------------------------------------
+
+// Propensities of all channels into a[] (sign = critical); lane partial sums.
+template <class Grp, class Pop>
+TL_D void pass_props(const Grp& g, const SimParams& p, const MView& mv, const float* rate,
+                     const Pop* x, float* a, float& pa, float& pac) {
+    const bool cc = flag(p.flags, TL_FLAG_COMPAT_CRIT);
+    float s = 0.f, sc = 0.f;
+    for (int j = g.rank(); j < p.M; j += g.size()) {
+        float aj;
+        bool crit;
+        propensity<Pop>(mv.chan[j], __ldg(rate + j), x, p.nc, cc, aj, crit);
+        a[j] = crit ? -aj : aj;
+        s += aj;
+        sc += crit ? aj : 0.f;
+    }
+    pa = s;
+    pac = sc;
+}
+
+// CGP bound of species i from its CSR row; optional moments out.
+template <class Pop>
+TL_D float species_bound(const SimParams& p, const MView& mv, const Pop* x, const float* a, int i,
+                         float mu, float s2) {
+    const bool cg = flag(p.flags, TL_FLAG_COMPAT_G);
+    const float xi = (float)x[i];
+    float gi;
+    if (cg) {
+        const int ord = i < p.M ? mv.chan[i].w : 0;
+        gi = (ord >= 1 && ord <= 3) ? (ord == 3 ? 2.f + 1.f / (xi - 1.f) : (float)ord) : 0.f;
+    } else {
+        gi = g_of(mv.gkind[i], xi);
+    }
+    const float num = fmaxf(p.eps * xi / gi, 1.f);
+    const float b1 = num / fabsf(mu);
+    const float b2 = num * num / fabsf(s2);
+    return fminf(b1, b2);
+}
+
+template <bool OUT, class Grp, class Pop>
+TL_D float pass_tau(const Grp& g, const SimParams& p, const MView& mv, const Pop* x, const float* a,
+                    float* mu_out, float* s2_out) {
+    const bool all_rows = flag(p.flags, TL_FLAG_COMPAT_STOICH);
+    float tmin = kInfF;
+    if constexpr (Grp::kWidth == 0) {
+        // one warp per species row, lanes stride the row's entries
+        for (int i = g.warp; i < p.N; i += g.nwarps) {
+            if (!all_rows && mv.gkind[i] == 0 && !OUT) continue;
+            float mu = 0.f, s2 = 0.f;
+            const int e = mv.rp[i + 1];
+            for (int q = mv.rp[i] + g.lane; q < e; q += 32) {
+                const int pk = mv.vc[q];
+                const float aj = a[unpack_idx(pk)];
+                if (!is_crit(aj)) {
+                    const float v = (float)unpack_v(pk);
+                    const float t = v * aj;
+                    mu += t;
+                    s2 += v * t;
+                }
+            }
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+                mu += __shfl_xor_sync(0xffffffffu, mu, o);
+                s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+            }
+            if (g.lane == 0) {
+                if (OUT) {
+                    mu_out[i] = mu;
+                    s2_out[i] = s2;
+                }
+                if (all_rows || mv.gkind[i] != 0) tmin = fminf(tmin, species_bound<Pop>(p, mv, x, a, i, mu, s2));
+            }
+        }
+    } else {
+        for (int i = g.rank(); i < p.N; i += g.size()) {
+            if (!all_rows && mv.gkind[i] == 0 && !OUT) continue;
+            float mu = 0.f, s2 = 0.f;
+            const int e = mv.rp[i + 1];
+            for (int q = mv.rp[i]; q < e; ++q) {
+                const int pk = mv.vc[q];
+                const float aj = a[unpack_idx(pk)];
+                if (!is_crit(aj)) {
+                    const float v = (float)unpack_v(pk);
+                    const float t = v * aj;
+                    mu += t;
+                    s2 += v * t;
+                }
+            }
+            if (OUT) {
+                mu_out[i] = mu;
+                s2_out[i] = s2;
+            }
+            if (all_rows || mv.gkind[i] != 0) tmin = fminf(tmin, species_bound<Pop>(p, mv, x, a, i, mu, s2));
+        }
+    }
+    return g.minf(tmin);
+}
+
+// xn = x + V k (k stored as int in a[]); returns true if any xn < 0 (or the
+// population type overflows, which also sets *ovf).
+template <class Grp, class Pop>
+TL_D bool pass_update(const Grp& g, const SimParams& p, const MView& mv, const Pop* x, const int* k,
+                      Pop* xn, bool& ovf) {
+    bool neg = false, of = false;
+    if constexpr (Grp::kWidth == 0) {
+        for (int i = g.warp; i < p.N; i += g.nwarps) {
+            long long d = 0;
+            const int e = mv.urp[i + 1];
+            for (int q = mv.urp[i] + g.lane; q < e; q += 32) {
+                const int pk = mv.uvc[q];
+                d += (long long)unpack_v(pk) * (long long)k[unpack_idx(pk)];
+            }
+#pragma unroll
+            for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+            if (g.lane == 0) {
+                const long long nx = (long long)x[i] + d;
+                if (sizeof(Pop) == 4 && nx > 2147483647LL) of = true;
+                xn[i] = (Pop)nx;
+                neg |= nx < 0;
+            }
+        }
+    } else {
+        for (int i = g.rank(); i < p.N; i += g.size()) {
+            long long d = 0;
+            const int e = mv.urp[i + 1];
+            for (int q = mv.urp[i]; q < e; ++q) {
+                const int pk = mv.uvc[q];
+                d += (long long)unpack_v(pk) * (long long)k[unpack_idx(pk)];
+            }
+            const long long nx = (long long)x[i] + d;
+            if (sizeof(Pop) == 4 && nx > 2147483647LL) of = true;
+            xn[i] = (Pop)nx;
+            neg |= nx < 0;
+        }
+    }
+    ovf = g.any(of);
+    return g.any(neg || of);
+}
+
+// Draw a channel with probability a_j / total among channels whose
+// criticality matches `want` (want: 0 = all channels, 1 = critical only).
+// Channels are taken in lane-major order: lane l owns j = l, l+G, ... .  The
+// cumulative sums across lanes are FP64; inside a lane the FP32 partial sum
+// is replayed in the same order it was accumulated, so the lane intervals
+// tile [0, total) exactly as the totals were formed.
+template <class Grp, class AccT>
+TL_D int select_channel(const Grp& g, const SimParams& p, const float* a, float lane_part, AccT target,
+                        int want_crit) {
+    const AccT part = (AccT)lane_part;
+    AccT excl;
+    if constexpr (Grp::kWidth == 1) {
+        excl = 0;
+    } else {
+        excl = (AccT)g.excl_scan((double)part);
+    }
+    const bool mine = (part > (AccT)0) && (target < excl + part);
+    int L = g.first(mine);
+    if (L < 0) L = g.last(part > (AccT)0);
+    int sel = -1;
+    if (g.rank() == L) {
+        float acc = 0.f;
+        int lastpos = -1;
+        for (int j = g.rank(); j < p.M; j += g.size()) {
+            const float aj = a[j];
+            const bool c = is_crit(aj);
+            if (want_crit && !c) continue;
+            const float v = fabsf(aj);
+            if (!(v > 0.f)) continue;
+            acc += v;
+            lastpos = j;
+            if (target < excl + (AccT)acc) {
+                sel = j;
+                break;
+            }
+        }
+        if (sel < 0) sel = lastpos;
+    }
+    if constexpr (Grp::kWidth == 1) {
+        return sel;
+    } else {
+        return g.bcast(sel, L < 0 ? 0 : L);
+    }
+}
+
+// Lane partial sum of critical propensities in the same order select uses.
+// (pass_props already returns it as pac.)
+
+template <class Grp, class Pop>
+TL_D void record_point(const Grp& g, const SimParams& p, const Pop* x, Pop* samp, int kpt) {
+    Pop* dst = samp + (size_t)kpt * p.K;
+    for (int q = g.rank(); q < p.K; q += g.size()) dst[q] = x[p.tracked[q]];
+}
+
+// ---------------------------------------------------------------------------
+// One step of one realization: a tau-leap (with rejection + halving) or a
+// block of direct-method steps (model.cu:301-413).
+// ---------------------------------------------------------------------------
+template <class Grp, class Pop, class TimeT, bool SENS>
+TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& s, int set, uint32_t r,
+                  Pop* samp, float* score, RState<TimeT>& st) {
+    const float* rate = p.rates + (size_t)set * p.M;
+    const double T = p.t_final[set];
+    const unsigned f = p.flags;
+
+    float pa, pac;
+    pass_props<Grp, Pop>(g, p, mv, rate, s.x, s.a, pa, pac);
+    g.sync();
+    TimeT a0 = (TimeT)g.sumd((double)pa);
+    if (!(a0 > (TimeT)0)) {
+        // nothing can fire: the state holds to t_final
+        while (st.kpt <= p.n_int) record_point<Grp, Pop>(g, p, s.x, samp, st.kpt++);
+        st.t = (TimeT)T;
+        st.done = 1;
+        return;
+    }
+    const TimeT a0c = (TimeT)g.sumd((double)pac);
+    float tau1 = pass_tau<false, Grp, Pop>(g, p, mv, s.x, s.a, nullptr, nullptr);
+
+    if ((double)tau1 * (double)a0 < (double)p.ssa_factor) {
+        // ---- direct-method block (CGP 2006 step 2; model.cu:334-345) ----
+        for (int q = 0; q < p.ssa_block; ++q) {
+            if (q > 0) {
+                pass_props<Grp, Pop>(g, p, mv, rate, s.x, s.a, pa, pac);
+                g.sync();
+                a0 = (TimeT)g.sumd((double)pa);
+                if (!(a0 > (TimeT)0)) {
+                    while (st.kpt <= p.n_int) record_point<Grp, Pop>(g, p, s.x, samp, st.kpt++);
+                    if (SENS) {
+                        // no channel can fire: the survival term is zero
+                    }
+                    st.t = (TimeT)T;
+                    st.done = 1;
+                    return;
+                }
+            }
+            const U4 w = step_words(p.k0, p.k1, st.step, r, (uint32_t)set);
+            const TimeT target = (TimeT)u01d(w.z, w.w) * a0;
+            const int j = select_channel<Grp, TimeT>(g, p, s.a, pa, target, 0);
+            TimeT dt;
+            if (flag(f, TL_FLAG_COMPAT_TAU2)) {
+                dt = (TimeT)(-logf(u01f(w.x))) / (TimeT)fabsf(s.a[j]);
+            } else {
+                dt = (TimeT)(-logf(u01f(w.x))) / a0;
+            }
+            while (st.kpt <= p.n_int && st.t + dt >= grid_time<TimeT>(p, T, st.kpt))
+                record_point<Grp, Pop>(g, p, s.x, samp, st.kpt++);
+            if (st.kpt > p.n_int) {
+                if (SENS) {
+                    const float rem = (float)((TimeT)T - st.t);
+                    for (int m = g.rank(); m < p.M; m += g.size()) {
+                        const float c = __ldg(rate + m);
+                        if (c > 0.f) score[m] -= fabsf(s.a[m]) * rem / c;
+                    }
+                }
+                st.t = (TimeT)T;
+                st.done = 1;
+                g.sync();
+                return;
+            }
+            if (SENS) {
+                const float dtf = (float)dt;
+                for (int m = g.rank(); m < p.M; m += g.size()) {
+                    const float c = __ldg(rate + m);
+                    if (c > 0.f) score[m] += ((m == j ? 1.f : 0.f) - fabsf(s.a[m]) * dtf) / c;
+                }
+            }
+            g.sync();
+            if (!flag(f, TL_FLAG_COMPAT_SSA) && j >= 0) {
+                const int e = mv.cp[j + 1];
+                for (int q2 = mv.cp[j] + g.rank(); q2 < e; q2 += g.size()) {
+                    const int pk = mv.rv[q2];
+                    s.x[unpack_idx(pk)] += (Pop)unpack_v(pk);
+                }
+            }
+            g.sync();
+            st.t += dt;
+            st.step++;
+            st.ssa++;
+            st.nsteps++;
+            if (p.max_steps > 0 && st.nsteps >= p.max_steps) return;
+        }
+        return;
+    }
+
+    // ---- tau-leap with negative-population rejection (CGP 2006 steps 3-5) ----
+    const TimeT t_next = grid_time<TimeT>(p, T, st.kpt);
+    TimeT tau;
+    bool clamp;
+    for (int attempt = 0;; ++attempt) {
+        const U4 w = step_words(p.k0, p.k1, st.step, r, (uint32_t)set);
+        int jc = -1;
+        float tau2 = kInfF;
+        if (a0c > (TimeT)0) {
+            if (flag(f, TL_FLAG_COMPAT_TAU2)) {
+                jc = select_channel<Grp, TimeT>(g, p, s.a, pac, (TimeT)u01d(w.z, w.w) * a0c, 1);
+                tau2 = -logf(u01f(w.x)) / fabsf(s.a[jc]);
+            } else {
+                tau2 = (float)((TimeT)(-logf(u01f(w.x))) / a0c);
+            }
+        }
+        tau = (TimeT)fminf(tau1, tau2);
+        bool fire = tau2 < tau1;
+        clamp = false;
+        if (st.t + tau >= t_next) {
+            tau = t_next - st.t;
+            clamp = true;
+            fire = false;
+        }
+        if (fire && jc < 0) jc = select_channel<Grp, TimeT>(g, p, s.a, pac, (TimeT)u01d(w.z, w.w) * a0c, 1);
+        if (!fire) jc = -1;
+        const float tauf = (float)tau;
+        // Poisson firing counts (model.cu:458-549), written over a[] as ints
+        int* kk = reinterpret_cast<int*>(s.a);
+        for (int j = g.rank(); j < p.M; j += g.size()) {
+            const float aj = s.a[j];
+            int k;
+            if (is_crit(aj)) {
+                k = (j == jc) ? 1 : 0;
+            } else {
+                const float mu = aj * tauf;
+                ChanRng rng;
+                rng.init((uint32_t)j, st.step, r, (uint32_t)set, p.k0, p.k1);
+                k = flag(f, TL_FLAG_COMPAT_POISSON) ? poisson_reference(mu, rng) : poisson_cgp(mu, rng);
+            }
+            kk[j] = k;
+        }
+        g.sync();
+        bool ovf = false;
+        const bool bad = pass_update<Grp, Pop>(g, p, mv, s.x, kk, s.xn, ovf);
+        if (ovf) {
+            if (g.leader()) atomicOr((unsigned*)(p.ctr + 5), kErrOverflow);
+            st.done = 1;
+            while (st.kpt <= p.n_int) record_point<Grp, Pop>(g, p, s.x, samp, st.kpt++);
+            return;
+        }
+        if (!bad) break;
+        // reject: halve tau1, fresh counters, same state
+        st.step++;
+        st.rej++;
+        tau1 *= 0.5f;
+        g.sync();
+        pass_props<Grp, Pop>(g, p, mv, rate, s.x, s.a, pa, pac);
+        g.sync();
+        if (attempt >= 64) {
+            if (g.leader()) atomicOr((unsigned*)(p.ctr + 5), kErrHalving);
+            st.done = 1;
+            while (st.kpt <= p.n_int) record_point<Grp, Pop>(g, p, s.x, samp, st.kpt++);
+            return;
+        }
+    }
+    if (SENS) {
+        // score_j += (k_j - a_j*tau)/c_j with a_j recomputed from the old state
+        const bool cc = flag(f, TL_FLAG_COMPAT_CRIT);
+        const float tauf = (float)tau;
+        const int* kk = reinterpret_cast<const int*>(s.a);
+        for (int m = g.rank(); m < p.M; m += g.size()) {
+            const float c = __ldg(rate + m);
+            if (c > 0.f) {
+                float am;
+                bool cr;
+                propensity<Pop>(mv.chan[m], c, s.x, p.nc, cc, am, cr);
+                score[m] += ((float)kk[m] - am * tauf) / c;
+            }
+        }
+    }
+    g.sync();
+    {
+        Pop* t = s.x;
+        s.x = s.xn;
+        s.xn = t;
+    }
+    st.t = clamp ? t_next : st.t + tau;
+    st.step++;
+    st.leaps++;
+    st.nsteps++;
+    if (clamp) {
+        record_point<Grp, Pop>(g, p, s.x, samp, st.kpt);
+        st.kpt++;
+        if (st.kpt > p.n_int) st.done = 1;
+    }
+    g.sync();
+}
+
+}  // namespace tl

@@ -1,0 +1,38 @@
+// tl_launch.h - host launchers of the kernels, one set per population type
+// (Pop = int for 32-bit, long long for 64-bit populations).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace tl {
+
+struct SimParams;
+
+// kind: 1 = thread, 32 = warp, 0 = CTA per realization.
+template <class Pop>
+cudaError_t launch_fused(const SimParams& p, int kind, bool sens, int block, int grid, size_t smem,
+                         cudaStream_t st);
+template <class Pop>
+cudaError_t fused_occupancy(int kind, bool sens, int block, size_t smem, int* blocks_per_sm);
+template <class Pop>
+cudaError_t launch_plain_init(const SimParams& p, cudaStream_t st);
+template <class Pop>
+cudaError_t launch_plain_step(const SimParams& p, float* a_all, cudaStream_t st);
+cudaError_t launch_plain_tally(const SimParams& p, cudaStream_t st);
+template <class Pop>
+cudaError_t launch_stats(const void* samp, long long R, int P, int K, int S, double* mean, double* sd,
+                         cudaStream_t st);
+template <class Pop>
+cudaError_t launch_grad(const void* samp, const float* scores, long long R, int P, int K, int M, int S,
+                        double* grad, double* se, double* meanf, cudaStream_t st);
+template <class Pop>
+cudaError_t launch_eval(const SimParams& p, const long long* x, int n, float* a, unsigned char* crit, float* mu,
+                        float* s2, float* tau, double* a0, size_t smem, cudaStream_t st);
+template <class Pop>
+cudaError_t launch_replay(const SimParams& p, const long long* x0, const int* k, int n_leaps, long long* x_out,
+                          int* status, size_t smem, cudaStream_t st);
+cudaError_t launch_philox(const void* ctr, const void* key, int n, void* out, cudaStream_t st);
+cudaError_t launch_poisson(const float* mean, int n, unsigned k0, unsigned k1, unsigned step, int compat,
+                           int* out, cudaStream_t st);
+
+}  // namespace tl

@@ -1,0 +1,148 @@
+"""Simulation-level parity of the CUDA path with the FP64 oracle.
+
+Statistical checks use fixed seeds, so each is deterministic; the
+acceptance level is 99% (p > 0.01) unless stated otherwise.
+"""
+import numpy as np
+import pytest
+from scipy import stats
+
+from oracle import py as ora
+from tau_leaping_gb300 import Model, _ffi
+
+pytestmark = pytest.mark.gpu
+
+P99 = 0.01
+
+
+def dimer(s1=2000):
+    return Model.generate("dimer", x0_min=s1, x0_max=s1)
+
+
+def compare_final(a, b, label, p=P99):
+    """a, b: [R, K] samples at t_final.  Welch t-test on means, Levene on
+    variances, two-sample KS on each tracked species."""
+    for k in range(a.shape[1]):
+        x, y = a[:, k].astype(float), b[:, k].astype(float)
+        pt = stats.ttest_ind(x, y, equal_var=False).pvalue
+        pl = stats.levene(x, y).pvalue
+        pk = stats.ks_2samp(x, y).pvalue
+        assert pt > p and pl > p and pk > p, f"{label} species {k}: t {pt:.3g} levene {pl:.3g} ks {pk:.3g}"
+
+
+@pytest.mark.parametrize("variant", [_ffi.VARIANT_THREAD, _ffi.VARIANT_WARP, _ffi.VARIANT_CTA, _ffi.VARIANT_PLAIN])
+def test_dimer_tau_leap_matches_oracle(variant):
+    m = dimer()
+    o = ora.OracleModel.from_desc(m.desc())
+    T = 2.0
+    g = m.simulate(T, 20000, seed=5, intervals=4, tracked=[0, 1], variant=variant, keep_samples=True)
+    r = o.simulate(T, 4000, seed=99, intervals=4, tracked=[0, 1], threads=8)
+    assert g.truncated == 0
+    assert g.leaps > 0 and g.ssa_steps > 0
+    compare_final(g.samples[0, :, -1, :], r["samples"][0, :, -1, :], f"variant {variant}")
+    # intermediate grid point too
+    compare_final(g.samples[0, :, 2, :], r["samples"][0, :, 2, :], f"variant {variant} t=T/2")
+    # the device reduction equals the host reduction of the same samples
+    s = g.samples[0].astype(np.float64)
+    assert np.allclose(g.mean[0], s.mean(0), rtol=1e-12)
+    assert np.allclose(g.stddev[0], s.std(0, ddof=1), rtol=1e-9)
+    assert np.allclose(g.times[0], [0, 0.5, 1.0, 1.5, 2.0])
+
+
+def test_dimer_tau_leap_close_to_exact_ssa():
+    m = dimer(1000)
+    o = ora.OracleModel.from_desc(m.desc())
+    T = 1.0
+    g = m.simulate(T, 100000, seed=3, tracked=[0, 1], keep_samples=True)
+    r = o.simulate(T, 20000, seed=4, tracked=[0, 1], method=1, threads=8)
+    a, b = g.samples[0, :, -1, :].astype(float), r["samples"][0, :, -1, :].astype(float)
+    for k in range(2):
+        ma, mb = a[:, k].mean(), b[:, k].mean()
+        se = np.sqrt(a[:, k].var() / len(a) + b[:, k].var() / len(b))
+        # tau-leaping bias (eps = 0.03) + 4 standard errors
+        assert abs(ma - mb) <= 0.01 * abs(mb) + 4 * se, (k, ma, mb, se)
+        va, vb = a[:, k].var(ddof=1), b[:, k].var(ddof=1)
+        sev = vb * np.sqrt(2 / len(b) + 2 / len(a))
+        assert abs(va - vb) <= 0.02 * vb + 4 * sev, (k, va, vb)
+
+
+def test_deterministic_and_variant_independent_streams():
+    m = dimer()
+    kw = dict(t_final=1.0, n=512, seed=9, tracked=[0, 1], keep_samples=True, intervals=2)
+    a = m.simulate(variant=_ffi.VARIANT_WARP, **kw)
+    b = m.simulate(variant=_ffi.VARIANT_WARP, **kw)
+    assert np.array_equal(a.samples, b.samples)
+    assert (a.leaps, a.ssa_steps, a.rejections) == (b.leaps, b.ssa_steps, b.rejections)
+    c = m.simulate(variant=_ffi.VARIANT_WARP, block_threads=64, **kw)
+    assert np.array_equal(a.samples, c.samples), "scheduling must not change a realization"
+
+
+def test_rate_sets_are_independent_of_batch_neighbours():
+    m = dimer()
+    base = m.desc()["rate"]
+    sets1 = np.stack([base, base * 1.5])
+    sets2 = np.stack([base, base * 0.5, base * 2.0])
+    kw = dict(t_final=1.0, n=256, seed=4, tracked=[0, 1], keep_samples=True)
+    a = m.simulate(rate_sets=sets1, t_final_sets=[1.0, 0.5], **kw)
+    b = m.simulate(rate_sets=sets2, t_final_sets=[1.0, 2.0, 3.0], **kw)
+    assert np.array_equal(a.samples[0], b.samples[0])
+    assert np.allclose(a.times[1], [0.0, 0.5])
+
+
+def test_edge_cases():
+    # nothing can fire: the state holds
+    m = Model.from_arrays([0, 0], [1.0], [0, 2], [0, 1], [-1, 1])
+    r = m.simulate(5.0, 16, intervals=3, keep_samples=True)
+    assert r.leaps == 0 and r.ssa_steps == 0
+    assert not r.samples.any()
+    # single realization, zero rate channel, source channel (no reactant)
+    m2 = Model.from_arrays([10, 0], [0.0, 2.0], [0, 2, 3], [0, 1, 1], [-1, 1, 1])
+    r2 = m2.simulate(3.0, 1, intervals=3, keep_samples=True, tracked=[0, 1])
+    assert r2.samples[0, 0, :, 0].tolist() == [10, 10, 10, 10]
+    assert r2.samples[0, 0, -1, 1] > 0
+    # step cap: reported and every realization truncated
+    m3 = dimer()
+    r3 = m3.simulate(10.0, 64, max_steps=5, allow_truncation=True, tracked=[0])
+    assert r3.status == 5 and r3.truncated == 64
+    with pytest.raises(_ffi.TLError) as e:
+        m3.simulate(10.0, 64, max_steps=5, tracked=[0])
+    assert e.value.status == 5
+    # invalid configuration
+    for bad in (dict(t_final=-1.0, n=4), dict(t_final=1.0, n=0), dict(t_final=1.0, n=4, intervals=0),
+                dict(t_final=1.0, n=4, tracked=[7])):
+        with pytest.raises(_ffi.TLError) as e:
+            m3.simulate(**bad)
+        assert e.value.status == 1
+
+
+def test_int32_overflow_detected():
+    # S1 -> 2 S1 from 2^30: doubles past int32 within t=2
+    m = Model.from_arrays([2**30], [1.0], [0, 1], [0], [1], pop_bits=32)
+    with pytest.raises(_ffi.TLError) as e:
+        m.simulate(2.0, 4, tracked=[0])
+    assert e.value.status == 4
+    m64 = Model.from_arrays([2**30], [1.0], [0, 1], [0], [1], pop_bits=64)
+    r = m64.simulate(1.0, 64, tracked=[0])
+    assert abs(r.mean[0, -1, 0] / (2**30 * np.e) - 1) < 1e-3
+
+
+def test_chain_mixed_precision_error_vs_ssa():
+    m = Model.generate("chain", n_species=64)
+    o = ora.OracleModel.from_desc(m.desc())
+    tr = list(range(0, 64, 8))
+    g = m.simulate(1.0, 20000, seed=2, tracked=tr, keep_samples=True)
+    r = o.simulate(1.0, 4000, seed=3, tracked=tr, method=1, threads=8)
+    a, b = g.samples[0, :, -1, :].astype(float), r["samples"][0, :, -1, :].astype(float)
+    rel_mean = np.abs(a.mean(0) - b.mean(0)) / b.mean(0)
+    se = np.sqrt(a.var(0) / len(a) + b.var(0) / len(b)) / b.mean(0)
+    assert np.all(rel_mean <= 0.01 + 4 * se), rel_mean
+
+
+def test_colloid_cta_matches_oracle():
+    m = Model.generate("colloid", n_species=60)
+    o = ora.OracleModel.from_desc(m.desc())
+    g = m.simulate(0.01, 2048, seed=6, tracked=[0, 1, 9], variant=_ffi.VARIANT_CTA, keep_samples=True)
+    w = m.simulate(0.01, 2048, seed=6, tracked=[0, 1, 9], variant=_ffi.VARIANT_WARP, keep_samples=True)
+    r = o.simulate(0.01, 1024, seed=7, tracked=[0, 1, 9], threads=8)
+    compare_final(g.samples[0, :, -1, :], r["samples"][0, :, -1, :], "colloid cta")
+    compare_final(w.samples[0, :, -1, :], r["samples"][0, :, -1, :], "colloid warp")
