@@ -531,6 +531,7 @@ TL_D void pass_props(const Grp& g, const SimParams& p, const MView& mv, const fl
         float aj;
         bool crit;
         propensity<Pop>(mv.chan[j], __ldg(rate + j), x, p.nc, cc, aj, crit);
+        aj = fabsf(aj);  // 2S-> at x=0 gives -0.0; the sign bit carries criticality
         a[j] = crit ? -aj : aj;
         s += aj;
         sc += crit ? aj : 0.f;

@@ -149,3 +149,28 @@ def test_poisson_reference_sampler_matches_oracle_law():
         s = poisson(np.full(100_000, mu, np.float32), seed=2, compat=True).astype(np.float64)
         r = ora.poisson(np.full(100_000, mu), seed=2, compat=True).astype(np.float64)
         assert abs(s.mean() - r.mean()) < 6 * np.sqrt(2 * mu / 1e5)
+
+
+GOLD_MODELS = {"dimer": ("dimer", {}), "toy": ("toy", {}), "chain64": ("chain", dict(n_species=64)),
+               "colloid40": ("colloid", dict(n_species=40))}
+
+
+@pytest.mark.parametrize("name", list(GOLD_MODELS))
+def test_device_matches_reference_functor_fixtures(name):
+    """tests/golden/ref_functors.npz holds the reference's own FP32 outputs
+    (IsCriticalAndPropensity, CompTau, FireReactionsFn).  With the compat
+    switches the device evaluates the same FP32 expressions in the same
+    order, so propensities are bit-identical; tau1 may differ by FMA
+    contraction only (relative 1e-6)."""
+    from pathlib import Path
+    g = np.load(Path(__file__).resolve().parent / "golden" / "ref_functors.npz")
+    fam, kw = GOLD_MODELS[name]
+    m = Model.generate(fam, **kw)
+    flags = _ffi.FLAG_COMPAT_G | _ffi.FLAG_COMPAT_CRIT | _ffi.FLAG_COMPAT_STOICH
+    d = m.eval_leap(g[f"{name}/x"], eps=0.03, flags=flags)
+    assert np.array_equal(d["crit"], g[f"{name}/crit"])
+    assert np.array_equal(d["a"], g[f"{name}/a"])
+    t_ref = g[f"{name}/tau1"].astype(np.float64)
+    assert np.max(np.abs(d["tau1"] - t_ref) / t_ref) <= 1e-6
+    out = m.replay(g[f"{name}/x_fire0"], g[f"{name}/k"], raw=True)
+    assert np.array_equal(out, g[f"{name}/fired"])

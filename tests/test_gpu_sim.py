@@ -116,12 +116,12 @@ def test_edge_cases():
 
 
 def test_int32_overflow_detected():
-    # S1 -> 2 S1 from 2^30: doubles past int32 within t=2
-    m = Model.from_arrays([2**30], [1.0], [0, 1], [0], [1], pop_bits=32)
+    # S1 -> 2 S1 from 2^30: grows past int32 within t=2
+    m = Model.from_arrays([2**30], [1.0], [0, 2], [0, 0], [-1, 2], pop_bits=32)
     with pytest.raises(_ffi.TLError) as e:
         m.simulate(2.0, 4, tracked=[0])
     assert e.value.status == 4
-    m64 = Model.from_arrays([2**30], [1.0], [0, 1], [0], [1], pop_bits=64)
+    m64 = Model.from_arrays([2**30], [1.0], [0, 2], [0, 0], [-1, 2], pop_bits=64)
     r = m64.simulate(1.0, 64, tracked=[0])
     assert abs(r.mean[0, -1, 0] / (2**30 * np.e) - 1) < 1e-3
 
