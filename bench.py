@@ -119,7 +119,7 @@ def model_bytes(m) -> tuple[int, int]:
     N, M, nn, nr = m.n_species, m.n_channels, m.nnz_net, m.nnz_raw
     a16 = lambda b: (b + 15) // 16 * 16  # noqa: E731
     w = 8 if m.pop_bits == 64 else 4
-    blob = (a16(16 * M) + a16(N) + a16(4 * (N + 1)) + a16(4 * nn) + a16(4 * (M + 1)) + a16(4 * nn) +
+    blob = (a16(16 * M) + a16(N) + a16(4 * N) + a16(4 * (N + 1)) + a16(4 * nn) + a16(4 * (M + 1)) + a16(4 * nn) +
             a16(4 * (N + 1)) + a16(4 * nr))
     return blob + N * w + 4 * M, w
 

@@ -9,12 +9,28 @@ REF="$1"; OUT="$2"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 CUDA_INC=/usr/local/cuda/include
 mkdir -p "$OUT"
-if [ -f "$OUT/libtlref.so" ] && [ "$OUT/libtlref.so" -nt "$HERE/ref/harness.cpp" ] && [ "$OUT/libtlref.so" -nt "$HERE/ref/shim.h" ]; then
-  exit 0
+if [ ! -f "$OUT/libtlref.so" ] || [ "$HERE/ref/harness.cpp" -nt "$OUT/libtlref.so" ] || [ "$HERE/ref/shim.h" -nt "$OUT/libtlref.so" ]; then
+  g++ -std=c++17 -O1 -fPIC -shared -w -DNDEBUG \
+    -DTHRUST_DEVICE_SYSTEM=THRUST_DEVICE_SYSTEM_CPP -D__global__= \
+    -I"$REF" -I"$REF/tau_leaping" -I"$CUDA_INC" -I"$CUDA_INC/cccl" \
+    -include "$HERE/ref/shim.h" \
+    "$HERE/ref/harness.cpp" -o "$OUT/libtlref.so"
+  echo "built $OUT/libtlref.so"
 fi
-g++ -std=c++17 -O1 -fPIC -shared -w -DNDEBUG \
-  -DTHRUST_DEVICE_SYSTEM=THRUST_DEVICE_SYSTEM_CPP -D__global__= \
-  -I"$REF" -I"$REF/tau_leaping" -I"$CUDA_INC" -I"$CUDA_INC/cccl" \
-  -include "$HERE/ref/shim.h" \
-  "$HERE/ref/harness.cpp" -o "$OUT/libtlref.so"
-echo "built $OUT/libtlref.so"
+
+# The reference's whole host path + a driver with logging on -> ref_driver.
+DRV="$OUT/ref_driver"
+if [ ! -f "$DRV" ] || [ "$HERE/ref/driver.cpp" -nt "$DRV" ] || [ "$HERE/ref/shim_full.h" -nt "$DRV" ] || [ "$HERE/ref/stubs.cpp" -nt "$DRV" ]; then
+  OBJ="$OUT/obj"; mkdir -p "$OBJ"
+  FLAGS="-std=c++17 -O2 -w -DNDEBUG -DTHRUST_DEVICE_SYSTEM=THRUST_DEVICE_SYSTEM_CPP -D__global__= -I$REF -I$REF/tau_leaping -I$CUDA_INC -I$CUDA_INC/cccl -include $HERE/ref/shim_full.h"
+  pids=()
+  for src in model.cu model.cpp ModelConst.cu ModelState.cu CSRMatrixPacked.cu CSRMatrix.cu CSCMatrix.cu \
+             CSCHostMatrixData.cpp StochKitReader.cpp functions.cpp statistics.cpp; do
+    g++ $FLAGS -x c++ -c "$REF/tau_leaping/$src" -o "$OBJ/${src}.o" & pids+=($!)
+  done
+  g++ $FLAGS -x c++ -c "$HERE/ref/driver.cpp" -o "$OBJ/driver.o" & pids+=($!)
+  g++ -std=c++17 -O2 -w -I$CUDA_INC -c "$HERE/ref/stubs.cpp" -o "$OBJ/stubs.o" & pids+=($!)
+  for p in "${pids[@]}"; do wait "$p"; done
+  g++ -o "$DRV" "$OBJ"/*.o
+  echo "built $DRV"
+fi

@@ -17,8 +17,10 @@
 //   direct-method step                  tau_leaping/model.cu:427-451
 // plus an exact direct-method SSA (Gillespie 1977) for statistical checks.
 // Random numbers come from its own Philox4x32-10 (Salmon et al. SC'11) with
-// the engine's counter layout (channel|0xFFFFFFFF, step, realization,
-// set<<8|block), so both sides draw from the same streams.
+// the engine's counter layout: step scalars (0xFFFFFFFF, step, r, set<<8),
+// first Poisson words of channels 4g..4g+3 (g, step, r, set<<8|0xFF), and
+// further per-channel uniforms (j, step, r, set<<8|b), so both sides draw
+// from the same streams.
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -71,8 +73,31 @@ struct Stream {
     }
 };
 
-// Poisson(mu): inversion below 10, Hormann's PTRS (1993) above.
-int64_t poisson(double mu, Stream& s) {
+// Poisson(mu): inversion below 10, Hormann's PTRS (1993) above.  For mu <
+// 10 the first uniform is q = (w + 1/2) 2^-32 from the channel's word of the
+// shared block: K = 0 iff q >= 1 - exp(-mu); otherwise the inversion goes on
+// with u = 1 - q from k = 1.  Further uniforms come from the private stream.
+int64_t poisson_inv(double mu, Stream& s);
+int64_t poisson(double mu, uint32_t w, Stream& s) {
+    if (!(mu > 0.0)) return 0;
+    if (mu < 10.0) {
+        const double q = ((double)w + 0.5) / 4294967296.0;
+        if (q >= -std::expm1(-mu)) return 0;
+        const double u = 1.0 - q;
+        double p = std::exp(-mu), F = p;
+        for (int k = 1; k < 200; ++k) {
+            p *= mu / (double)k;
+            const double Fn = F + p;
+            if (u <= Fn) return k;
+            if (Fn == F) break;
+            F = Fn;
+        }
+        return poisson_inv(mu, s);
+    }
+    return poisson_inv(mu, s);
+}
+
+int64_t poisson_inv(double mu, Stream& s) {
     if (!(mu > 0.0)) return 0;
     if (mu < 10.0) {
         for (;;) {
@@ -328,7 +353,9 @@ void ora_philox(const uint32_t* ctr, const uint32_t* key, int n, uint32_t* out) 
 int ora_poisson(const double* mean, int n, uint64_t seed, uint32_t step, int compat, int64_t* out) {
     for (int i = 0; i < n; ++i) {
         Stream s{(uint32_t)i, step, 0u, 0u, (uint32_t)seed, (uint32_t)(seed >> 32)};
-        out[i] = compat ? poisson_ref(mean[i], s) : poisson(mean[i], s);
+        const W4 gw = philox(W4{(uint32_t)i >> 2, step, 0u, 0xFFu}, (uint32_t)seed, (uint32_t)(seed >> 32));
+        const uint32_t w0 = (i & 3) == 0 ? gw.x : (i & 3) == 1 ? gw.y : (i & 3) == 2 ? gw.z : gw.w;
+        out[i] = compat ? poisson_ref(mean[i], s) : poisson(mean[i], w0, s);
     }
     return 0;
 }
@@ -494,12 +521,16 @@ void run_one(const ora_model& m, const ora_cfg& c, int set, uint32_t r, int64_t*
             }
             if (fire && jc < 0) jc = pick(uni52(w.z, w.w) * a0c, true);
             if (!fire) jc = -1;
+            W4 gw{0, 0, 0, 0};
             for (int j = 0; j < M; ++j) {
+                if ((j & 3) == 0)
+                    gw = philox(W4{(uint32_t)j >> 2, step, r, ((uint32_t)set << 8) | 0xFFu}, k0, k1);
                 if (crit[j]) {
                     kk[j] = j == jc;
                 } else {
                     Stream s{(uint32_t)j, step, r, (uint32_t)set << 8, k0, k1};
-                    kk[j] = (f & F_COMPAT_POISSON) ? poisson_ref(a[j] * tau, s) : poisson(a[j] * tau, s);
+                    const uint32_t w0 = (j & 3) == 0 ? gw.x : (j & 3) == 1 ? gw.y : (j & 3) == 2 ? gw.z : gw.w;
+                    kk[j] = (f & F_COMPAT_POISSON) ? poisson_ref(a[j] * tau, s) : poisson(a[j] * tau, w0, s);
                 }
             }
             bool neg = false;

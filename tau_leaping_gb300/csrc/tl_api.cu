@@ -72,6 +72,7 @@ static tl_status upload(tl_model* m) {
     };
     d.off_chan = sect((size_t)M * 16);
     d.off_gkind = sect((size_t)N);
+    d.off_perm = sect((size_t)N * 4);
     d.off_rp = sect((size_t)(N + 1) * 4);
     d.off_vc = sect((size_t)d.nnz_net * 4);
     d.off_cp = sect((size_t)(M + 1) * 4);
@@ -85,6 +86,7 @@ static tl_status upload(tl_model* m) {
     for (int j = 0; j < M; ++j)
         chan[j] = make_int4(h.s0[(size_t)j], h.s1[(size_t)j], h.order[(size_t)j], h.ref_order[(size_t)j]);
     memcpy(hb.data() + d.off_gkind, h.gkind.data(), (size_t)N);
+    memcpy(hb.data() + d.off_perm, h.rowperm.data(), (size_t)N * 4);
     memcpy(hb.data() + d.off_rp, h.net_rp.data(), (size_t)(N + 1) * 4);
     if (d.nnz_net) memcpy(hb.data() + d.off_vc, h.net_vc.data(), (size_t)d.nnz_net * 4);
     memcpy(hb.data() + d.off_cp, h.net_cp.data(), (size_t)(M + 1) * 4);
@@ -133,6 +135,7 @@ static MView global_view(const tl_model* m, bool raw_mu, bool raw_update) {
     MView v;
     v.chan = reinterpret_cast<const int4*>(b + d.off_chan);
     v.gkind = reinterpret_cast<const signed char*>(b + d.off_gkind);
+    v.perm = reinterpret_cast<const int*>(b + d.off_perm);
     const int* nrp = reinterpret_cast<const int*>(b + d.off_rp);
     const int* nvc = reinterpret_cast<const int*>(b + d.off_vc);
     const int* rrp = reinterpret_cast<const int*>(b + d.off_raw_rp);
@@ -409,6 +412,7 @@ static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad
     p.stage_bytes = pl.stage;
     p.off_chan = m->d.off_chan;
     p.off_gkind = m->d.off_gkind;
+    p.off_perm = m->d.off_perm;
     p.off_rp = m->d.off_rp;
     p.off_vc = m->d.off_vc;
     p.off_cp = m->d.off_cp;

@@ -200,6 +200,40 @@ TL_D int poisson_cgp(float mu, Rng& rng) {
     return poisson_ptrs(mu, rng);
 }
 
+// Shared first words: channels 4g..4g+3 of one step take their first 32-bit
+// word from one Philox block (g, step, r, set<<8 | 0xFF); the private
+// stream (j, step, r, set<<8 | b), b < 0xFF, supplies any further uniforms.
+TL_HD U4 group_words(uint32_t k0, uint32_t k1, uint32_t g, uint32_t step, uint32_t r, uint32_t set) {
+    return philox10(U4{g, step, r, (set << 8) | 0xFFu}, k0, k1);
+}
+
+// Poisson(mu) from one 32-bit word w for mu < 10: q = (w + 1/2) 2^-32 is
+// uniform on (0,1) with full relative precision near 0, so the k = 0 test
+// q >= P(K >= 1) = -expm1(-mu) stays exact for tiny means (a 23-bit
+// uniform would quantise it); k >= 1 continues the sequential inversion on
+// u = 1 - q.  mu >= 10 uses PTRS on the private stream.
+template <class Rng>
+TL_D int poisson_first(float mu, uint32_t w, Rng& rng) {
+    if (!(mu > 0.f)) return 0;
+    if (mu >= 10.f) return poisson_ptrs(mu, rng);
+    const float q = ((float)w + 0.5f) * 2.3283064365386963e-10f;
+    // P(K >= 1) = 1 - exp(-mu); Taylor series below 0.01 (error < mu^4/24)
+    const float s0 = mu < 0.01f ? mu * (1.f - mu * (0.5f - mu * (1.f / 6.f))) : -expm1f(-mu);
+    if (q >= s0) return 0;
+    const float u = 1.f - q;
+    float p = expf(-mu), F = p;
+    for (int k = 1; k < 64; ++k) {
+        p = p * __fdividef(mu, (float)k);
+        const float Fn = F + p;
+        if (u <= Fn) return k;
+        if (Fn == F) break;  // u above the representable mass: draw afresh
+        F = Fn;
+    }
+    return poisson_inversion(mu, rng);
+}
+
+TL_D uint32_t word_of(const U4& w, int e) { return e == 0 ? w.x : e == 1 ? w.y : e == 2 ? w.z : w.w; }
+
 // The reference's sampler (model.cu:477-520, functions.h:37-54): Knuth's
 // product method below mean 80 capped at 300 firings, |Normal(mean, mean)|
 // from the polar Box-Muller draw above, truncated toward zero.
@@ -448,6 +482,7 @@ struct GCta {
 struct MView {
     const int4* chan;         // [M] {s0, s1, order, reference order}
     const signed char* gkind; // [N]
+    const int* perm;          // [N] row processing order (longest rows first)
     const int* rp;            // [N+1] CSR used for mu/sigma^2
     const int* vc;            // [nnz] packed (col<<3)|((v+2)&7)
     const int* urp;           // [N+1] CSR used for the update (net entries)
@@ -483,7 +518,7 @@ struct SimParams {
     // staging of the constant blob into shared memory
     const unsigned char* blob;
     int stage_bytes;    // 0 = no staging
-    int off_chan, off_gkind, off_rp, off_vc, off_cp, off_rv;  // byte offsets (net)
+    int off_chan, off_gkind, off_perm, off_rp, off_vc, off_cp, off_rv;  // byte offsets (net)
     int slot_bytes;     // per group
     unsigned long long* ctr; // [0] work, [1] leaps, [2] ssa, [3] rejections,
                              // [4] truncated, [5] error bits, [6] done count
@@ -594,7 +629,8 @@ TL_D float pass_tau(const Grp& g, const SimParams& p, const MView& mv, const Pop
             }
         }
     } else {
-        for (int i = g.rank(); i < p.N; i += g.size()) {
+        for (int ii = g.rank(); ii < p.N; ii += g.size()) {
+            const int i = mv.perm[ii];
             if (!all_rows && mv.gkind[i] == 0 && !OUT) continue;
             float mu = 0.f, s2 = 0.f;
             const int e = mv.rp[i + 1];
@@ -642,7 +678,8 @@ TL_D bool pass_update(const Grp& g, const SimParams& p, const MView& mv, const P
             }
         }
     } else {
-        for (int i = g.rank(); i < p.N; i += g.size()) {
+        for (int ii = g.rank(); ii < p.N; ii += g.size()) {
+            const int i = mv.perm[ii];
             long long d = 0;
             const int e = mv.urp[i + 1];
             for (int q = mv.urp[i]; q < e; ++q) {
@@ -713,6 +750,57 @@ TL_D void record_point(const Grp& g, const SimParams& p, const Pop* x, Pop* samp
     for (int q = g.rank(); q < p.K; q += g.size()) dst[q] = x[p.tracked[q]];
 }
 
+// Poisson firing counts of one leap (model.cu:458-549), written over a[] as
+// ints.  A thread takes four consecutive channels at a time so that they
+// share one Philox block for their first uniforms.
+template <class Grp>
+TL_D void pass_fire(const Grp& g, const SimParams& p, float* a, float tauf, int jc, uint32_t step, uint32_t r,
+                    uint32_t set) {
+    const bool refs = flag(p.flags, TL_FLAG_COMPAT_POISSON);
+    const bool vec = (reinterpret_cast<uintptr_t>(a) & 15) == 0;
+    int* kk = reinterpret_cast<int*>(a);
+    for (int g4 = g.rank(); 4 * g4 < p.M; g4 += g.size()) {
+        const int j0 = 4 * g4;
+        const bool full = vec && j0 + 3 < p.M;
+        float av[4];
+        if (full) {
+            const float4 v = *reinterpret_cast<const float4*>(a + j0);
+            av[0] = v.x;
+            av[1] = v.y;
+            av[2] = v.z;
+            av[3] = v.w;
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e) av[e] = j0 + e < p.M ? a[j0 + e] : -0.f;
+        }
+        bool need = false;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) need |= !is_crit(av[e]) && av[e] * tauf > 0.f;
+        U4 gw{0u, 0u, 0u, 0u};
+        if (need && !refs) gw = group_words(p.k0, p.k1, (uint32_t)g4, step, r, set);
+        int kv[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int j = j0 + e;
+            if (is_crit(av[e])) {
+                kv[e] = (j == jc) ? 1 : 0;
+            } else {
+                const float mu = av[e] * tauf;
+                ChanRng rng;
+                rng.init((uint32_t)j, step, r, set, p.k0, p.k1);
+                kv[e] = refs ? poisson_reference(mu, rng) : poisson_first(mu, word_of(gw, e), rng);
+            }
+        }
+        if (full) {
+            *reinterpret_cast<int4*>(kk + j0) = make_int4(kv[0], kv[1], kv[2], kv[3]);
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (j0 + e < p.M) kk[j0 + e] = kv[e];
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // One step of one realization: a tau-leap (with rejection + halving) or a
 // block of direct-method steps (model.cu:301-413).
@@ -727,24 +815,26 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
     float pa, pac;
     pass_props<Grp, Pop>(g, p, mv, rate, s.x, s.a, pa, pac);
     g.sync();
-    TimeT a0 = (TimeT)g.sumd((double)pa);
-    if (!(a0 > (TimeT)0)) {
+    const float a0f = g.sumf(pa);  // FP32: only the branch test and tau2 use it
+    if (!(a0f > 0.f)) {
         // nothing can fire: the state holds to t_final
         while (st.kpt <= p.n_int) record_point<Grp, Pop>(g, p, s.x, samp, st.kpt++);
         st.t = (TimeT)T;
         st.done = 1;
         return;
     }
-    const TimeT a0c = (TimeT)g.sumd((double)pac);
     float tau1 = pass_tau<false, Grp, Pop>(g, p, mv, s.x, s.a, nullptr, nullptr);
 
-    if ((double)tau1 * (double)a0 < (double)p.ssa_factor) {
+    if (tau1 * a0f < p.ssa_factor) {
         // ---- direct-method block (CGP 2006 step 2; model.cu:334-345) ----
         for (int q = 0; q < p.ssa_block; ++q) {
             if (q > 0) {
                 pass_props<Grp, Pop>(g, p, mv, rate, s.x, s.a, pa, pac);
                 g.sync();
-                a0 = (TimeT)g.sumd((double)pa);
+            }
+            // total for the cumulative search: FP64 over the lane partials
+            const TimeT a0 = (TimeT)g.sumd((double)pa);
+            {
                 if (!(a0 > (TimeT)0)) {
                     while (st.kpt <= p.n_int) record_point<Grp, Pop>(g, p, s.x, samp, st.kpt++);
                     if (SENS) {
@@ -810,14 +900,16 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
     bool clamp;
     for (int attempt = 0;; ++attempt) {
         const U4 w = step_words(p.k0, p.k1, st.step, r, (uint32_t)set);
+        const float a0cf = g.sumf(pac);
         int jc = -1;
         float tau2 = kInfF;
-        if (a0c > (TimeT)0) {
+        if (a0cf > 0.f) {
             if (flag(f, TL_FLAG_COMPAT_TAU2)) {
+                const TimeT a0c = (TimeT)g.sumd((double)pac);
                 jc = select_channel<Grp, TimeT>(g, p, s.a, pac, (TimeT)u01d(w.z, w.w) * a0c, 1);
                 tau2 = -logf(u01f(w.x)) / fabsf(s.a[jc]);
             } else {
-                tau2 = (float)((TimeT)(-logf(u01f(w.x))) / a0c);
+                tau2 = -logf(u01f(w.x)) / a0cf;
             }
         }
         tau = (TimeT)fminf(tau1, tau2);
@@ -828,24 +920,14 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
             clamp = true;
             fire = false;
         }
-        if (fire && jc < 0) jc = select_channel<Grp, TimeT>(g, p, s.a, pac, (TimeT)u01d(w.z, w.w) * a0c, 1);
+        if (fire && jc < 0) {
+            const TimeT a0c = (TimeT)g.sumd((double)pac);
+            jc = select_channel<Grp, TimeT>(g, p, s.a, pac, (TimeT)u01d(w.z, w.w) * a0c, 1);
+        }
         if (!fire) jc = -1;
         const float tauf = (float)tau;
-        // Poisson firing counts (model.cu:458-549), written over a[] as ints
+        pass_fire<Grp>(g, p, s.a, tauf, jc, st.step, r, (uint32_t)set);
         int* kk = reinterpret_cast<int*>(s.a);
-        for (int j = g.rank(); j < p.M; j += g.size()) {
-            const float aj = s.a[j];
-            int k;
-            if (is_crit(aj)) {
-                k = (j == jc) ? 1 : 0;
-            } else {
-                const float mu = aj * tauf;
-                ChanRng rng;
-                rng.init((uint32_t)j, st.step, r, (uint32_t)set, p.k0, p.k1);
-                k = flag(f, TL_FLAG_COMPAT_POISSON) ? poisson_reference(mu, rng) : poisson_cgp(mu, rng);
-            }
-            kk[j] = k;
-        }
         g.sync();
         bool ovf = false;
         const bool bad = pass_update<Grp, Pop>(g, p, mv, s.x, kk, s.xn, ovf);

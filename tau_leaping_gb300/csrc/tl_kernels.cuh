@@ -85,6 +85,7 @@ TL_D MView staged_view(const unsigned char* s, const SimParams& p) {
     MView v;
     v.chan = reinterpret_cast<const int4*>(s + p.off_chan);
     v.gkind = reinterpret_cast<const signed char*>(s + p.off_gkind);
+    v.perm = reinterpret_cast<const int*>(s + p.off_perm);
     v.rp = reinterpret_cast<const int*>(s + p.off_rp);
     v.vc = reinterpret_cast<const int*>(s + p.off_vc);
     v.urp = v.rp;
@@ -433,7 +434,13 @@ __global__ void k_poisson(const float* mean, int n, uint32_t k0, uint32_t k1, ui
     if (i >= n) return;
     ChanRng rng;
     rng.init((uint32_t)i, step, 0u, 0u, k0, k1);
-    out[i] = compat ? poisson_reference(mean[i], rng) : poisson_cgp(mean[i], rng);
+    if (compat) {
+        out[i] = poisson_reference(mean[i], rng);
+    } else {
+        // exactly the hot path's draw for channel i of realization 0, set 0
+        const U4 gw = group_words(k0, k1, (uint32_t)i >> 2, step, 0u, 0u);
+        out[i] = poisson_first(mean[i], word_of(gw, i & 3), rng);
+    }
 }
 #endif
 

@@ -215,6 +215,13 @@ tl_status derive_tables(HostModel& h, std::string& err) {
     h.net_rv.resize(nrows.size());
     for (size_t q = 0; q < nrows.size(); ++q) h.net_rv[q] = pack(nrows[q], nvals[q]);
     to_rows(N, M, h.net_cp, nrows, nvals, h.net_rp, h.net_vc);
+    // processing order of species rows: longest first, so the rows a warp
+    // walks side by side have similar lengths
+    h.rowperm.resize((size_t)N);
+    for (int i = 0; i < N; ++i) h.rowperm[(size_t)i] = i;
+    std::stable_sort(h.rowperm.begin(), h.rowperm.end(), [&](int a, int b) {
+        return h.net_rp[(size_t)a + 1] - h.net_rp[(size_t)a] > h.net_rp[(size_t)b + 1] - h.net_rp[(size_t)b];
+    });
     if ((int)h.names.size() != N) {
         h.names.resize((size_t)N);
         for (int i = 0; i < N; ++i) h.names[(size_t)i] = "S" + std::to_string(i + 1);
