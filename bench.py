@@ -53,7 +53,30 @@ WORKLOADS = {
     "colloid": dict(family="colloid", t_final=0.01, R=4096, tracked=[0, 1],
                     desc="colloidal aggregation 250 species x 31250 channels (seed 13), t_final 0.01, "
                          "4096 realizations, int64"),
+    "batch": dict(family="batch", t_final=None, R=None, tracked=[0, 1],
+                  desc="one launch: dimer-decay 64 rate sets (c x lognormal(0,0.2), seed 17) x 4096 realizations, "
+                       "t_final U[1,10]; toy network 16 rate sets x 1024 realizations, t_final U[0.05,0.1]; "
+                       "likelihood-ratio sensitivities on"),
 }
+
+
+def batch_items(seed=1, scale=1.0):
+    """The sensitivity + uneven-batch workload: dimer-decay (S1 = 1e5) with
+    64 rate sets scaled by lognormal(0, 0.2) from seed 17, 4096 realizations
+    each, t_final uniform in [1, 10]; the toy network with 16 sets, 1024
+    realizations each, t_final uniform in [0.05, 0.1]."""
+    from tau_leaping_gb300 import Model
+    rng = np.random.default_rng(17)
+    dim, toy = Model.generate("dimer"), Model.generate("toy")
+    ds = dim.desc()["rate"][None, :] * rng.lognormal(0.0, 0.2, size=(64, 4))
+    dt = rng.uniform(1.0, 10.0, size=64)
+    ts = toy.desc()["rate"][None, :] * rng.lognormal(0.0, 0.2, size=(16, toy.n_channels))
+    tt = rng.uniform(0.05, 0.1, size=16)
+    n1, n2 = max(1, int(4096 * scale)), max(1, int(1024 * scale))
+    return [dict(model=dim, t_final=10.0, n=n1, seed=seed, tracked=[0, 1], rate_sets=ds, t_final_sets=dt,
+                 sensitivity=True),
+            dict(model=toy, t_final=0.1, n=n2, seed=seed, tracked=[0, 4], rate_sets=ts, t_final_sets=tt,
+                 sensitivity=True)], (dim, toy)
 
 
 def peaks() -> dict:
@@ -132,12 +155,56 @@ def alg_bytes_per_step(m) -> int:
     return 4 * m.nnz_net + 4 * m.nnz_net + 13 * m.n_channels + 4 * (m.n_species + 1) + 2 * w * m.n_species
 
 
+def run_batch_workload(args, wl, rank, world, local_rank):
+    """C5: sensitivity + uneven batching in one launch (tl_simulate_batch)."""
+    import torch
+
+    from tau_leaping_gb300 import _ffi
+    from tau_leaping_gb300.model import simulate_batch
+    torch.cuda.set_device(local_rank)
+    _ffi.check(_ffi.lib().tl_set_device(local_rank), "tl_set_device")
+    items, (dim, toy) = batch_items(args.seed, args.batch_scale)
+    stream = torch.cuda.current_stream()
+    sptr = C.c_void_p(stream.cuda_stream)
+    for it in items:
+        it["realization_offset"] = rank * it["n"]
+    for _ in range(args.warmup):
+        simulate_batch(items, stream=sptr)
+    torch.cuda.synchronize()
+    times, outs = [], []
+    with Clocks(local_rank) as clk:
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            o = simulate_batch(items, stream=sptr)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            outs.append(o)
+    tot = float(sum(times))
+    steps = sum(it["leaps"] + it["ssa_steps"] for o in outs for it in o)
+    o = outs[-1]
+    line = {"metric": METRIC, "value": steps / (tot / 1e3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tot / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32+int32", "data": "synthetic (seeded generator)",
+            "config": {"workload": wl["desc"], "variant": "batched (lane units + warp units)",
+                       "grid": o[0]["grid"], "block_threads": o[0]["block_threads"]},
+            "leaps_per_step": float(sum(it["leaps"] for it in o)),
+            "ssa_steps_per_step": float(sum(it["ssa_steps"] for it in o)),
+            "gpu_launches": args.steps * (1 + 2 * len(items)),
+            "kernel_ms": o[0]["kernel_ms"], "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_ours(args, wl, rank, world, local_rank):
     import torch
 
     from tau_leaping_gb300 import Model, _ffi
     from tau_leaping_gb300.model import _ptr
 
+    if wl["family"] == "batch":
+        return run_batch_workload(args, wl, rank, world, local_rank)
     torch.cuda.set_device(local_rank)
     _ffi.check(_ffi.lib().tl_set_device(local_rank), "tl_set_device")
     m = Model.generate(wl["family"])
@@ -310,6 +377,7 @@ def main():
     ap.add_argument("--variant", type=int, default=0)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--batch-scale", type=float, default=1.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

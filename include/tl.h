@@ -237,6 +237,26 @@ typedef struct tl_result {
  */
 tl_status tl_simulate(tl_model *m, const tl_run_cfg *cfg, tl_result *res);
 
+/*
+ * Several (model, configuration) pairs in ONE persistent launch.  Each item
+ * is simulated exactly as tl_simulate would (same streams, same outputs in
+ * its result; grad non-NULL adds tl_sensitivity's gradients).  Small models
+ * (<= 16 species and channels) run 32 realizations per warp, one per lane;
+ * larger ones one realization per warp; every warp takes work from one
+ * counter, so rate sets with uneven step counts or t_final balance out.
+ * Models must share the device and the population width; variant and
+ * stream fields of the items' cfg are ignored (stream is the argument).
+ */
+typedef struct tl_batch_item {
+    tl_model *model;
+    const tl_run_cfg *cfg;
+    tl_result *result;     /* may be NULL                                   */
+    struct tl_grad_result *grad; /* non-NULL: sensitivities for this item   */
+} tl_batch_item;
+
+tl_status tl_simulate_batch(tl_batch_item *items, int32_t n_items,
+                            void *stream);
+
 /* ------------------------------------------------------------------------ */
 /* Sensitivity ("backward")                                                 */
 /* ------------------------------------------------------------------------ */
@@ -296,6 +316,23 @@ tl_status tl_philox(const uint32_t *ctr, const uint32_t *key, int32_t n,
  */
 tl_status tl_poisson(const float *mean, int32_t n, uint64_t seed,
                      uint32_t step, int32_t compat, int32_t *out);
+
+/* ------------------------------------------------------------------------ */
+/* Sharding across processes / GPUs                                         */
+/* ------------------------------------------------------------------------ */
+
+/*
+ * Merge per-shard statistics of disjoint realization ranges (each shard run
+ * with its own realization_offset) into the statistics of the union, with
+ * Chan, Golub and LeVeque's pairwise update of (count, mean, M2).
+ * means/stddevs: [n_parts][L]; counts: [n_parts]; stddev is the sample
+ * (n-1) deviation as tl_simulate returns it.  Host only, no device call.
+ * Replaces nothing in the reference (it never splits an ensemble).
+ */
+tl_status tl_merge_moments(int32_t n_parts, int32_t L, const int64_t *counts,
+                           const double *means, const double *stddevs,
+                           int64_t *count_out, double *mean_out,
+                           double *stddev_out);
 
 /* ------------------------------------------------------------------------ */
 /* Misc                                                                     */

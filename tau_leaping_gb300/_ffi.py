@@ -75,6 +75,10 @@ class GradResult(C.Structure):
     _fields_ = [("grad", P(c_dbl)), ("grad_stderr", P(c_dbl)), ("mean_final", P(c_dbl))]
 
 
+class BatchItem(C.Structure):
+    _fields_ = [("model", c_vp), ("cfg", P(RunCfg)), ("result", P(Result)), ("grad", P(GradResult))]
+
+
 # name -> (restype, argtypes); every symbol include/tl.h declares.
 SIGNATURES = {
     "tl_model_create": (c_i32, [P(ModelDesc), P(c_vp)]),
@@ -91,11 +95,13 @@ SIGNATURES = {
     "tl_run_cfg_init": (None, [P(RunCfg)]),
     "tl_simulate": (c_i32, [c_vp, P(RunCfg), P(Result)]),
     "tl_sensitivity": (c_i32, [c_vp, P(RunCfg), P(Result), P(GradResult)]),
+    "tl_simulate_batch": (c_i32, [P(BatchItem), c_i32, c_vp]),
     "tl_eval_leap": (c_i32, [c_vp, P(c_i64), c_i32, c_dbl, c_u32, c_i32, P(C.c_float), P(C.c_uint8),
                              P(C.c_float), P(C.c_float), P(C.c_float), P(c_dbl)]),
     "tl_replay": (c_i32, [c_vp, P(c_i64), P(c_i32), c_i32, c_i32, P(c_i64)]),
     "tl_philox": (c_i32, [P(c_u32), P(c_u32), c_i32, P(c_u32)]),
     "tl_poisson": (c_i32, [P(C.c_float), c_i32, c_u64, c_u32, c_i32, P(c_i32)]),
+    "tl_merge_moments": (c_i32, [c_i32, c_i32, P(c_i64), P(c_dbl), P(c_dbl), P(c_i64), P(c_dbl), P(c_dbl)]),
     "tl_status_str": (C.c_char_p, [c_i32]),
     "tl_last_error": (C.c_char_p, []),
     "tl_abi_version": (c_i32, []),

@@ -255,8 +255,31 @@ struct RunBuffers {
     float* a_all = nullptr;
 };
 
-static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad_result* grad) {
-    const auto t0 = std::chrono::steady_clock::now();
+// One (model, configuration) pair of a call: validation, scratch layout,
+// device parameters, reduction and result.
+struct Job {
+    tl_model* m = nullptr;
+    const tl_run_cfg* cfg = nullptr;
+    tl_result* res = nullptr;
+    tl_grad_result* grad = nullptr;
+    int S = 1, P = 2, K = 0;
+    long long R = 1, total = 1;
+    bool sens = false, keep = false, plain = false, compat_stoich = false;
+    size_t w = 4;
+    std::vector<float> hrates;
+    std::vector<double> htf;
+    Plan pl;
+    size_t o_rates = 0, o_tf = 0, o_tr = 0, o_samp = 0, o_sc = 0, o_ctr = 0, o_mean = 0, o_sd = 0, o_grad = 0,
+           o_gse = 0, o_gm = 0, o_ps = 0, o_pslot = 0, o_aall = 0;
+    RunBuffers rb;
+    SimParams p{};
+    std::vector<unsigned char> hs;
+    unsigned long long hc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+};
+
+static tl_status job_prepare(Job& J) {
+    tl_model* m = J.m;
+    const tl_run_cfg* cfg = J.cfg;
     if (!m || !cfg) {
         set_last_error("null model or config");
         return TL_ERR_INVALID_ARGUMENT;
@@ -286,115 +309,101 @@ static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad
         set_last_error("rate_sets is NULL");
         return TL_ERR_INVALID_ARGUMENT;
     }
-    const int S = std::max(1, cfg->n_rate_sets);
-    const long long R = cfg->n_realizations;
-    const int P = cfg->n_intervals + 1;
-    const int K = cfg->n_tracked;
-    const long long total = R * S;
-    const bool sens = grad != nullptr;
-    const bool keep = (cfg->flags & TL_FLAG_KEEP_SAMPLES) != 0;
-    const bool plain = cfg->variant == TL_VARIANT_PLAIN;
-    if (plain && sens) {
+    J.S = std::max(1, cfg->n_rate_sets);
+    J.R = cfg->n_realizations;
+    J.P = cfg->n_intervals + 1;
+    J.K = cfg->n_tracked;
+    J.total = J.R * J.S;
+    J.sens = J.grad != nullptr;
+    J.keep = (cfg->flags & TL_FLAG_KEEP_SAMPLES) != 0;
+    J.plain = cfg->variant == TL_VARIANT_PLAIN;
+    J.compat_stoich = (cfg->flags & TL_FLAG_COMPAT_STOICH) != 0;
+    J.w = h.pop_bits == 64 ? 8 : 4;
+    if (J.plain && J.sens) {
         set_last_error("the plain form has no sensitivity pass");
         return TL_ERR_UNSUPPORTED;
     }
-    if (sens && K < 1) {
+    if (J.sens && J.K < 1) {
         set_last_error("sensitivity needs at least one tracked species");
         return TL_ERR_INVALID_ARGUMENT;
     }
-    std::vector<float> hrates((size_t)S * M);
-    std::vector<double> htf((size_t)S, cfg->t_final);
-    for (int s = 0; s < S; ++s)
+    J.hrates.assign((size_t)J.S * M, 0.f);
+    J.htf.assign((size_t)J.S, cfg->t_final);
+    for (int s = 0; s < J.S; ++s)
         for (int j = 0; j < M; ++j) {
             const double c = cfg->n_rate_sets > 0 ? cfg->rate_sets[(size_t)s * M + j] : h.rate[(size_t)j];
             if (!std::isfinite(c) || c < 0.0) {
                 set_last_error("rate constants must be finite and >= 0");
                 return TL_ERR_NUMERIC;
             }
-            hrates[(size_t)s * M + j] = (float)c;
+            J.hrates[(size_t)s * M + j] = (float)c;
         }
     if (cfg->n_rate_sets > 0 && cfg->t_final_sets)
-        for (int s = 0; s < S; ++s) {
-            htf[(size_t)s] = cfg->t_final_sets[s];
-            if (!(htf[(size_t)s] > 0.0) || !std::isfinite(htf[(size_t)s])) {
+        for (int s = 0; s < J.S; ++s) {
+            J.htf[(size_t)s] = cfg->t_final_sets[s];
+            if (!(J.htf[(size_t)s] > 0.0) || !std::isfinite(J.htf[(size_t)s])) {
                 set_last_error("t_final_sets must be > 0");
                 return TL_ERR_INVALID_ARGUMENT;
             }
         }
-    {
-        tl_status ds = ensure_device(m);
-        if (ds != TL_OK) return ds;
-    }
-    TLC(cudaSetDevice(m->d.device));
-    cudaStream_t st = (cudaStream_t)cfg->stream;
-    const size_t w = h.pop_bits == 64 ? 8 : 4;
-    const bool compat_stoich = (cfg->flags & TL_FLAG_COMPAT_STOICH) != 0;
+    return ensure_device(m);
+}
 
-    Plan pl;
-    if (!plain) {
-        tl_status ps = make_plan(m, cfg->variant, cfg->block_threads, sens, compat_stoich, total, pl);
-        if (ps != TL_OK) return ps;
-    } else {
-        pl.variant = TL_VARIANT_PLAIN;
-        pl.kind = 1;
-        pl.block = 128;
-        pl.grid = (int)((total + 127) / 128);
-    }
+static void job_layout(Job& J, Carver& c) {
+    const int M = J.m->h.M, N = J.m->h.N, K1 = std::max(J.K, 1);
+    J.o_rates = c.take((size_t)J.S * M * 4);
+    J.o_tf = c.take((size_t)J.S * 8);
+    J.o_tr = c.take((size_t)K1 * 4);
+    J.o_samp = c.take((size_t)J.total * J.P * K1 * J.w);
+    J.o_sc = J.sens ? c.take((size_t)J.total * M * 4) : 0;
+    J.o_ctr = c.take(8 * 8);
+    J.o_mean = c.take((size_t)J.S * J.P * K1 * 8);
+    J.o_sd = c.take((size_t)J.S * J.P * K1 * 8);
+    J.o_grad = J.sens ? c.take((size_t)J.S * J.K * M * 8) : 0;
+    J.o_gse = J.sens ? c.take((size_t)J.S * J.K * M * 8) : 0;
+    J.o_gm = J.sens ? c.take((size_t)J.S * J.K * 8) : 0;
+    J.o_ps = J.plain ? c.take((size_t)J.total * 64) : 0;
+    J.o_pslot = J.plain ? c.take((size_t)J.total * 2 * N * J.w) : 0;
+    J.o_aall = J.plain ? c.take((size_t)J.total * M * 4) : 0;
+}
 
-    // scratch layout
-    Carver c;
-    const size_t o_rates = c.take((size_t)S * M * 4);
-    const size_t o_tf = c.take((size_t)S * 8);
-    const size_t o_tr = c.take((size_t)std::max(K, 1) * 4);
-    const size_t o_samp = c.take((size_t)total * P * std::max(K, 1) * w);
-    const size_t o_sc = sens ? c.take((size_t)total * M * 4) : 0;
-    const size_t o_ctr = c.take(8 * 8);
-    const size_t o_mean = c.take((size_t)S * P * std::max(K, 1) * 8);
-    const size_t o_sd = c.take((size_t)S * P * std::max(K, 1) * 8);
-    const size_t o_grad = sens ? c.take((size_t)S * K * M * 8) : 0;
-    const size_t o_gse = sens ? c.take((size_t)S * K * M * 8) : 0;
-    const size_t o_gm = sens ? c.take((size_t)S * K * 8) : 0;
-    const size_t o_ps = plain ? c.take((size_t)total * 64) : 0;
-    const size_t o_pslot = plain ? c.take((size_t)total * 2 * N * w) : 0;
-    const size_t o_aall = plain ? c.take((size_t)total * M * 4) : 0;
-    void* base = nullptr;
-    tl_status ss = scratch_get(m, c.off, &base);
-    if (ss != TL_OK) return ss;
-    unsigned char* B = reinterpret_cast<unsigned char*>(base);
-    RunBuffers rb;
-    rb.rates = reinterpret_cast<float*>(B + o_rates);
-    rb.tfin = reinterpret_cast<double*>(B + o_tf);
-    rb.tracked = reinterpret_cast<int*>(B + o_tr);
-    rb.samples = B + o_samp;
-    rb.scores = sens ? reinterpret_cast<float*>(B + o_sc) : nullptr;
-    rb.ctr = reinterpret_cast<unsigned long long*>(B + o_ctr);
-    rb.mean = reinterpret_cast<double*>(B + o_mean);
-    rb.sd = reinterpret_cast<double*>(B + o_sd);
-    if (sens) {
-        rb.grad = reinterpret_cast<double*>(B + o_grad);
-        rb.gse = reinterpret_cast<double*>(B + o_gse);
-        rb.gmean = reinterpret_cast<double*>(B + o_gm);
+static tl_status job_bind(Job& J, unsigned char* B, cudaStream_t st) {
+    tl_model* m = J.m;
+    const tl_run_cfg* cfg = J.cfg;
+    RunBuffers& rb = J.rb;
+    rb.rates = reinterpret_cast<float*>(B + J.o_rates);
+    rb.tfin = reinterpret_cast<double*>(B + J.o_tf);
+    rb.tracked = reinterpret_cast<int*>(B + J.o_tr);
+    rb.samples = B + J.o_samp;
+    rb.scores = J.sens ? reinterpret_cast<float*>(B + J.o_sc) : nullptr;
+    rb.ctr = reinterpret_cast<unsigned long long*>(B + J.o_ctr);
+    rb.mean = reinterpret_cast<double*>(B + J.o_mean);
+    rb.sd = reinterpret_cast<double*>(B + J.o_sd);
+    if (J.sens) {
+        rb.grad = reinterpret_cast<double*>(B + J.o_grad);
+        rb.gse = reinterpret_cast<double*>(B + J.o_gse);
+        rb.gmean = reinterpret_cast<double*>(B + J.o_gm);
     }
-    if (plain) {
-        rb.pstate = B + o_ps;
-        rb.pslots = B + o_pslot;
-        rb.a_all = reinterpret_cast<float*>(B + o_aall);
+    if (J.plain) {
+        rb.pstate = B + J.o_ps;
+        rb.pslots = B + J.o_pslot;
+        rb.a_all = reinterpret_cast<float*>(B + J.o_aall);
     }
-    TLC(cudaMemcpyAsync(rb.rates, hrates.data(), hrates.size() * 4, cudaMemcpyHostToDevice, st));
-    TLC(cudaMemcpyAsync(rb.tfin, htf.data(), htf.size() * 8, cudaMemcpyHostToDevice, st));
-    if (K > 0) TLC(cudaMemcpyAsync(rb.tracked, cfg->tracked, (size_t)K * 4, cudaMemcpyHostToDevice, st));
+    TLC(cudaMemcpyAsync(rb.rates, J.hrates.data(), J.hrates.size() * 4, cudaMemcpyHostToDevice, st));
+    TLC(cudaMemcpyAsync(rb.tfin, J.htf.data(), J.htf.size() * 8, cudaMemcpyHostToDevice, st));
+    if (J.K > 0) TLC(cudaMemcpyAsync(rb.tracked, cfg->tracked, (size_t)J.K * 4, cudaMemcpyHostToDevice, st));
     TLC(cudaMemsetAsync(rb.ctr, 0, 64, st));
-
-    SimParams p{};
-    p.N = N;
-    p.M = M;
-    p.g = global_view(m, compat_stoich, false);
+    SimParams& p = J.p;
+    p = SimParams{};
+    p.N = m->h.N;
+    p.M = m->h.M;
+    p.g = global_view(m, J.compat_stoich, false);
     p.x0 = m->d.x0;
     p.rates = rb.rates;
     p.t_final = rb.tfin;
-    p.R = R;
+    p.R = J.R;
     p.r_off = cfg->realization_offset;
-    p.S = S;
+    p.S = J.S;
     p.k0 = (uint32_t)(cfg->seed & 0xFFFFFFFFu);
     p.k1 = (uint32_t)(cfg->seed >> 32);
     p.eps = (float)cfg->eps;
@@ -402,14 +411,14 @@ static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad
     p.ssa_factor = (float)(cfg->ssa_factor > 0 ? cfg->ssa_factor : 10);
     p.ssa_block = cfg->ssa_block > 0 ? cfg->ssa_block : 100;
     p.n_int = cfg->n_intervals;
-    p.K = K;
+    p.K = J.K;
     p.tracked = rb.tracked;
     p.samples = rb.samples;
     p.scores = rb.scores;
     p.max_steps = cfg->max_steps;
     p.flags = cfg->flags;
     p.blob = m->d.blob;
-    p.stage_bytes = pl.stage;
+    p.stage_bytes = J.pl.stage;
     p.off_chan = m->d.off_chan;
     p.off_gkind = m->d.off_gkind;
     p.off_perm = m->d.off_perm;
@@ -421,6 +430,127 @@ static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad
     p.ctr = rb.ctr;
     p.pstate = rb.pstate;
     p.pslots = rb.pslots;
+    return TL_OK;
+}
+
+// Statistics / gradient reductions and the device-to-host copies.
+static tl_status job_reduce(Job& J, cudaStream_t st) {
+    const int M = J.m->h.M;
+    RunBuffers& rb = J.rb;
+    cudaError_t le;
+    if (J.K > 0) {
+        le = J.w == 8 ? launch_stats<long long>(rb.samples, J.R, J.P, J.K, J.S, rb.mean, rb.sd, st)
+                      : launch_stats<int>(rb.samples, J.R, J.P, J.K, J.S, rb.mean, rb.sd, st);
+        if (le != cudaSuccess) return cuda_fail(le, "statistics launch");
+    }
+    if (J.sens) {
+        le = J.w == 8 ? launch_grad<long long>(rb.samples, rb.scores, J.R, J.P, J.K, M, J.S, rb.grad, rb.gse, rb.gmean, st)
+                      : launch_grad<int>(rb.samples, rb.scores, J.R, J.P, J.K, M, J.S, rb.grad, rb.gse, rb.gmean, st);
+        if (le != cudaSuccess) return cuda_fail(le, "gradient launch");
+    }
+    TLC(cudaMemcpyAsync(J.hc, rb.ctr, 64, cudaMemcpyDeviceToHost, st));
+    const size_t SPK = (size_t)J.S * J.P * J.K;
+    if (J.res) {
+        if (J.res->mean && J.K > 0) TLC(cudaMemcpyAsync(J.res->mean, rb.mean, SPK * 8, cudaMemcpyDeviceToHost, st));
+        if (J.res->stddev && J.K > 0) TLC(cudaMemcpyAsync(J.res->stddev, rb.sd, SPK * 8, cudaMemcpyDeviceToHost, st));
+        if (J.res->samples && J.keep && J.K > 0) {
+            J.hs.resize((size_t)J.total * J.P * J.K * J.w);
+            TLC(cudaMemcpyAsync(J.hs.data(), rb.samples, J.hs.size(), cudaMemcpyDeviceToHost, st));
+        }
+    }
+    if (J.sens) {
+        tl_grad_result* g = J.grad;
+        const size_t SKM = (size_t)J.S * J.K * M;
+        if (g->grad) TLC(cudaMemcpyAsync(g->grad, rb.grad, SKM * 8, cudaMemcpyDeviceToHost, st));
+        if (g->grad_stderr) TLC(cudaMemcpyAsync(g->grad_stderr, rb.gse, SKM * 8, cudaMemcpyDeviceToHost, st));
+        if (g->mean_final)
+            TLC(cudaMemcpyAsync(g->mean_final, rb.gmean, (size_t)J.S * J.K * 8, cudaMemcpyDeviceToHost, st));
+    }
+    return TL_OK;
+}
+
+// After the stream is synchronised: fill the result, map error bits.
+static tl_status job_finish(Job& J, double kernel_ms, int launches, double total_ms) {
+    tl_result* res = J.res;
+    if (!J.hs.empty()) {
+        const size_t n = (size_t)J.total * J.P * J.K;
+        if (J.w == 8) memcpy(res->samples, J.hs.data(), n * 8);
+        else {
+            const int* src = reinterpret_cast<const int*>(J.hs.data());
+            for (size_t q = 0; q < n; ++q) res->samples[q] = src[q];
+        }
+    }
+    if (res) {
+        if (res->times)
+            for (int s = 0; s < J.S; ++s)
+                for (int k = 0; k < J.P; ++k)
+                    res->times[(size_t)s * J.P + k] = k == J.cfg->n_intervals
+                                                          ? J.htf[(size_t)s]
+                                                          : J.htf[(size_t)s] * (double)k / (double)J.cfg->n_intervals;
+        res->leaps = (int64_t)J.hc[1];
+        res->ssa_steps = (int64_t)J.hc[2];
+        res->rejections = (int64_t)J.hc[3];
+        res->truncated = (int64_t)J.hc[4];
+        res->kernel_ms = kernel_ms;
+        res->variant_used = J.pl.variant;
+        res->block_threads_used = J.pl.block;
+        res->grid_used = J.pl.grid;
+        res->launches = launches;
+        res->total_ms = total_ms;
+    }
+    const unsigned eb = (unsigned)J.hc[5];
+    if (eb & kErrWaitTimeout) {
+        set_last_error("shared-memory staging wait timed out");
+        return TL_ERR_WAIT_TIMEOUT;
+    }
+    if (eb & kErrOverflow) {
+        set_last_error("a population left the range of the population type");
+        return TL_ERR_OVERFLOW;
+    }
+    if (eb & (kErrHalving | kErrNumeric)) {
+        set_last_error("a leap could not be made non-negative by halving tau");
+        return TL_ERR_NUMERIC;
+    }
+    if (J.hc[4] > 0) {
+        set_last_error("max_steps reached; truncated realizations hold their last state");
+        return TL_ERR_STEP_CAP;
+    }
+    return TL_OK;
+}
+
+static double ms_since(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad_result* grad) {
+    const auto t0 = std::chrono::steady_clock::now();
+    Job J;
+    J.m = m;
+    J.cfg = cfg;
+    J.res = res;
+    J.grad = grad;
+    tl_status ps = job_prepare(J);
+    if (ps != TL_OK) return ps;
+    TLC(cudaSetDevice(m->d.device));
+    cudaStream_t st = (cudaStream_t)cfg->stream;
+    if (!J.plain) {
+        ps = make_plan(m, cfg->variant, cfg->block_threads, J.sens, J.compat_stoich, J.total, J.pl);
+        if (ps != TL_OK) return ps;
+    } else {
+        J.pl.variant = TL_VARIANT_PLAIN;
+        J.pl.kind = 1;
+        J.pl.block = 128;
+        J.pl.grid = (int)((J.total + 127) / 128);
+    }
+    Carver c;
+    job_layout(J, c);
+    void* base = nullptr;
+    ps = scratch_get(m, c.off, &base);
+    if (ps != TL_OK) return ps;
+    ps = job_bind(J, reinterpret_cast<unsigned char*>(base), st);
+    if (ps != TL_OK) return ps;
+    const SimParams& p = J.p;
+    const size_t w = J.w;
 
     cudaEvent_t e0, e1;
     TLC(cudaEventCreate(&e0));
@@ -428,9 +558,9 @@ static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad
     int launches = 0;
     cudaError_t le = cudaEventRecord(e0, st);
     if (le == cudaSuccess) {
-        if (!plain) {
-            le = w == 8 ? launch_fused<long long>(p, pl.kind, sens, pl.block, pl.grid, pl.smem, st)
-                        : launch_fused<int>(p, pl.kind, sens, pl.block, pl.grid, pl.smem, st);
+        if (!J.plain) {
+            le = w == 8 ? launch_fused<long long>(p, J.pl.kind, J.sens, J.pl.block, J.pl.grid, J.pl.smem, st)
+                        : launch_fused<int>(p, J.pl.kind, J.sens, J.pl.block, J.pl.grid, J.pl.smem, st);
             launches = 1;
         } else {
             le = w == 8 ? launch_plain_init<long long>(p, st) : launch_plain_init<int>(p, st);
@@ -439,13 +569,13 @@ static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad
             cudaMallocHost(&hdone, 8);
             while (le == cudaSuccess) {
                 for (int q = 0; q < 16 && le == cudaSuccess; ++q) {
-                    le = w == 8 ? launch_plain_step<long long>(p, rb.a_all, st) : launch_plain_step<int>(p, rb.a_all, st);
+                    le = w == 8 ? launch_plain_step<long long>(p, J.rb.a_all, st) : launch_plain_step<int>(p, J.rb.a_all, st);
                     ++launches;
                 }
                 if (le != cudaSuccess) break;
-                le = cudaMemcpyAsync(hdone, rb.ctr + 6, 8, cudaMemcpyDeviceToHost, st);
+                le = cudaMemcpyAsync(hdone, J.rb.ctr + 6, 8, cudaMemcpyDeviceToHost, st);
                 if (le == cudaSuccess) le = cudaStreamSynchronize(st);
-                if (le == cudaSuccess && *hdone >= (unsigned long long)total) break;
+                if (le == cudaSuccess && *hdone >= (unsigned long long)J.total) break;
                 if (launches > (1 << 26)) {  // a realization that never ends
                     cudaFreeHost(hdone);
                     cudaEventDestroy(e0);
@@ -465,86 +595,184 @@ static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad
         cudaEventDestroy(e1);
         return cuda_fail(le, "simulation launch");
     }
-    // statistics
-    if (K > 0) {
-        le = w == 8 ? launch_stats<long long>(rb.samples, R, P, K, S, rb.mean, rb.sd, st)
-                    : launch_stats<int>(rb.samples, R, P, K, S, rb.mean, rb.sd, st);
-        if (le != cudaSuccess) return cuda_fail(le, "statistics launch");
-    }
-    if (sens) {
-        le = w == 8 ? launch_grad<long long>(rb.samples, rb.scores, R, P, K, M, S, rb.grad, rb.gse, rb.gmean, st)
-                    : launch_grad<int>(rb.samples, rb.scores, R, P, K, M, S, rb.grad, rb.gse, rb.gmean, st);
-        if (le != cudaSuccess) return cuda_fail(le, "gradient launch");
-    }
-    unsigned long long hc[8];
-    TLC(cudaMemcpyAsync(hc, rb.ctr, 64, cudaMemcpyDeviceToHost, st));
-    if (res) {
-        if (res->mean && K > 0)
-            TLC(cudaMemcpyAsync(res->mean, rb.mean, (size_t)S * P * K * 8, cudaMemcpyDeviceToHost, st));
-        if (res->stddev && K > 0)
-            TLC(cudaMemcpyAsync(res->stddev, rb.sd, (size_t)S * P * K * 8, cudaMemcpyDeviceToHost, st));
-    }
-    std::vector<unsigned char> hs;
-    if (res && res->samples && keep && K > 0) {
-        hs.resize((size_t)total * P * K * w);
-        TLC(cudaMemcpyAsync(hs.data(), rb.samples, hs.size(), cudaMemcpyDeviceToHost, st));
-    }
-    if (sens) {
-        if (grad->grad) TLC(cudaMemcpyAsync(grad->grad, rb.grad, (size_t)S * K * M * 8, cudaMemcpyDeviceToHost, st));
-        if (grad->grad_stderr)
-            TLC(cudaMemcpyAsync(grad->grad_stderr, rb.gse, (size_t)S * K * M * 8, cudaMemcpyDeviceToHost, st));
-        if (grad->mean_final)
-            TLC(cudaMemcpyAsync(grad->mean_final, rb.gmean, (size_t)S * K * 8, cudaMemcpyDeviceToHost, st));
+    ps = job_reduce(J, st);
+    if (ps != TL_OK) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return ps;
     }
     TLC(cudaStreamSynchronize(st));
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (!hs.empty()) {
-        const size_t n = (size_t)total * P * K;
-        if (w == 8) memcpy(res->samples, hs.data(), n * 8);
-        else {
-            const int* src = reinterpret_cast<const int*>(hs.data());
-            for (size_t q = 0; q < n; ++q) res->samples[q] = src[q];
+    return job_finish(J, ms, launches, ms_since(t0));
+}
+
+// One launch over several (model, configuration) items.  Items of small
+// models run as lane units (32 realizations per warp, one per lane), the
+// others as warp units (one realization per warp); a warp takes units from
+// one global counter, so uneven step counts and uneven t_final balance out.
+static tl_status run_batch(tl_batch_item* items, int n, cudaStream_t st) {
+    const auto t0 = std::chrono::steady_clock::now();
+    if (!items || n < 1) {
+        set_last_error("empty batch");
+        return TL_ERR_INVALID_ARGUMENT;
+    }
+    std::vector<Job> jobs((size_t)n);
+    int device = -1, pop = 0;
+    for (int i = 0; i < n; ++i) {
+        Job& J = jobs[(size_t)i];
+        J.m = items[i].model;
+        J.cfg = items[i].cfg;
+        J.res = items[i].result;
+        J.grad = items[i].grad;
+        tl_status ps = job_prepare(J);
+        if (ps != TL_OK) return ps;
+        if (J.plain) {
+            set_last_error("the plain form cannot be batched");
+            return TL_ERR_UNSUPPORTED;
+        }
+        if (device < 0) {
+            device = J.m->d.device;
+            pop = J.m->h.pop_bits;
+        } else if (device != J.m->d.device || pop != J.m->h.pop_bits) {
+            set_last_error("batched models must share device and population width");
+            return TL_ERR_INVALID_ARGUMENT;
         }
     }
-    if (res) {
-        if (res->times)
-            for (int s = 0; s < S; ++s)
-                for (int k = 0; k < P; ++k)
-                    res->times[(size_t)s * P + k] =
-                        k == cfg->n_intervals ? htf[(size_t)s] : htf[(size_t)s] * (double)k / (double)cfg->n_intervals;
-        res->leaps = (int64_t)hc[1];
-        res->ssa_steps = (int64_t)hc[2];
-        res->rejections = (int64_t)hc[3];
-        res->truncated = (int64_t)hc[4];
-        res->kernel_ms = ms;
-        res->variant_used = pl.variant;
-        res->block_threads_used = pl.block;
-        res->grid_used = pl.grid;
-        res->launches = launches;
-        res->total_ms =
-            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    TLC(cudaSetDevice(device));
+    const int smax = max_smem_optin() - 2048;
+    // unit kind per item; the warp slot is the largest need
+    std::vector<int> lane(n);
+    size_t wslot = 0;
+    for (int i = 0; i < n; ++i) {
+        const tl_model* m = jobs[(size_t)i].m;
+        lane[(size_t)i] = (m->h.M <= 16 && m->h.N <= 16) ? 1 : 0;
+        const size_t need = lane[(size_t)i] ? 32 * slot_bytes(m) : slot_bytes(m);
+        wslot = std::max(wslot, need);
+        Plan& pl = jobs[(size_t)i].pl;
+        pl.variant = lane[(size_t)i] ? TL_VARIANT_THREAD : TL_VARIANT_WARP;
     }
-    const unsigned eb = (unsigned)hc[5];
-    if (eb & kErrWaitTimeout) {
-        set_last_error("shared-memory staging wait timed out");
-        return TL_ERR_WAIT_TIMEOUT;
+    wslot = al16(wslot);
+    const size_t spb = al16(sizeof(SimParams));
+    // stage every model's tables when they fit next to 4 warps' slots
+    std::vector<tl_model*> uniq;
+    for (auto& J : jobs)
+        if (std::find(uniq.begin(), uniq.end(), J.m) == uniq.end()) uniq.push_back(J.m);
+    size_t stage = 0;
+    std::vector<size_t> stage_off(uniq.size());
+    for (size_t u = 0; u < uniq.size(); ++u) {
+        stage_off[u] = stage;
+        stage += (size_t)uniq[u]->d.stage_bytes;
     }
-    if (eb & kErrOverflow) {
-        set_last_error("a population left the range of the population type");
-        return TL_ERR_OVERFLOW;
+    bool staged = true;
+    for (auto& J : jobs) staged &= !J.compat_stoich;
+    if (stage + 4 * (wslot + spb) > (size_t)smax) staged = false;
+    if (!staged) stage = 0;
+    int warps = 8;
+    while (warps > 1 && stage + (size_t)warps * (wslot + spb) > (size_t)smax) --warps;
+    if (stage + (size_t)warps * (wslot + spb) > (size_t)smax) {
+        set_last_error("a batched model is too large for a warp unit; run it with tl_simulate");
+        return TL_ERR_UNSUPPORTED;
     }
-    if (eb & (kErrHalving | kErrNumeric)) {
-        set_last_error("a leap could not be made non-negative by halving tau");
-        return TL_ERR_NUMERIC;
+    // scratch: every job's buffers, the item table, the staged tables, a counter
+    Carver c;
+    for (auto& J : jobs) job_layout(J, c);
+    const size_t o_items = c.take(sizeof(BatchItem) * (size_t)n);
+    const size_t o_stage = c.take(std::max<size_t>(stage, 16));
+    const size_t o_wctr = c.take(16);
+    tl_model* owner = jobs[0].m;
+    void* base = nullptr;
+    tl_status ps = scratch_get(owner, c.off, &base);
+    if (ps != TL_OK) return ps;
+    unsigned char* B = reinterpret_cast<unsigned char*>(base);
+    for (auto& J : jobs) {
+        ps = job_bind(J, B, st);
+        if (ps != TL_OK) return ps;
     }
-    if (hc[4] > 0) {
-        set_last_error("max_steps reached; truncated realizations hold their last state");
-        return TL_ERR_STEP_CAP;
+    if (staged)
+        for (size_t u = 0; u < uniq.size(); ++u)
+            TLC(cudaMemcpyAsync(B + o_stage + stage_off[u], uniq[u]->d.blob, (size_t)uniq[u]->d.stage_bytes,
+                                cudaMemcpyDeviceToDevice, st));
+    // unit table: warp-unit items first (longer realizations), then lane units
+    std::vector<int> order;
+    for (int i = 0; i < n; ++i)
+        if (!lane[(size_t)i]) order.push_back(i);
+    for (int i = 0; i < n; ++i)
+        if (lane[(size_t)i]) order.push_back(i);
+    std::vector<BatchItem> hb((size_t)n);
+    long long units = 0;
+    for (int k = 0; k < n; ++k) {
+        const int i = order[(size_t)k];
+        Job& J = jobs[(size_t)i];
+        BatchItem& b = hb[(size_t)k];
+        b.p = J.p;
+        b.p.stage_bytes = 0;
+        b.lane_mode = lane[(size_t)i];
+        b.unit_begin = units;
+        b.units = lane[(size_t)i] ? (J.total + 31) / 32 : J.total;
+        units += b.units;
+        b.stage_off = -1;
+        if (staged) {
+            const size_t u = (size_t)(std::find(uniq.begin(), uniq.end(), J.m) - uniq.begin());
+            b.stage_off = (int)stage_off[u];
+        }
+        J.pl.block = 32 * warps;
     }
-    return TL_OK;
+    TLC(cudaMemcpyAsync(B + o_items, hb.data(), sizeof(BatchItem) * (size_t)n, cudaMemcpyHostToDevice, st));
+    TLC(cudaMemsetAsync(B + o_wctr, 0, 16, st));
+    BatchParams bp{};
+    bp.items = reinterpret_cast<const BatchItem*>(B + o_items);
+    bp.n_items = n;
+    bp.total_units = units;
+    bp.stage_src = B + o_stage;
+    bp.stage_bytes = (int)stage;
+    bp.warp_slot_bytes = (int)wslot;
+    bp.params_bytes = (int)spb;
+    bp.wctr = reinterpret_cast<unsigned long long*>(B + o_wctr);
+    bool any_sens = false;
+    for (auto& J : jobs) any_sens |= J.sens;
+    const size_t smem = stage + (size_t)warps * (wslot + spb);
+    int bps = 0;
+    cudaError_t le = pop == 64 ? batch_occupancy<long long>(any_sens, 32 * warps, smem, &bps)
+                               : batch_occupancy<int>(any_sens, 32 * warps, smem, &bps);
+    if (le != cudaSuccess) return cuda_fail(le, "batch occupancy");
+    const int grid = (int)std::min<long long>((long long)sm_count() * std::max(bps, 1),
+                                              (units + warps - 1) / warps);
+    for (auto& J : jobs) J.pl.grid = grid;
+    cudaEvent_t e0, e1;
+    TLC(cudaEventCreate(&e0));
+    TLC(cudaEventCreate(&e1));
+    le = cudaEventRecord(e0, st);
+    if (le == cudaSuccess)
+        le = pop == 64 ? launch_batch<long long>(bp, any_sens, 32 * warps, grid, smem, st)
+                       : launch_batch<int>(bp, any_sens, 32 * warps, grid, smem, st);
+    if (le == cudaSuccess) le = cudaEventRecord(e1, st);
+    if (le != cudaSuccess) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return cuda_fail(le, "batch launch");
+    }
+    for (auto& J : jobs) {
+        ps = job_reduce(J, st);
+        if (ps != TL_OK) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return ps;
+        }
+    }
+    TLC(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    tl_status worst = TL_OK;
+    for (auto& J : jobs) {
+        const tl_status s2 = job_finish(J, ms, 1, ms_since(t0));
+        if (s2 != TL_OK && (worst == TL_OK || worst == TL_ERR_STEP_CAP)) worst = s2;
+    }
+    return worst;
 }
 
 }  // namespace tl
@@ -788,6 +1016,10 @@ void tl_run_cfg_init(tl_run_cfg* cfg) {
 
 tl_status tl_simulate(tl_model* m, const tl_run_cfg* cfg, tl_result* res) { return run(m, cfg, res, nullptr); }
 
+tl_status tl_simulate_batch(tl_batch_item* items, int32_t n_items, void* stream) {
+    return run_batch(items, n_items, (cudaStream_t)stream);
+}
+
 tl_status tl_sensitivity(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad_result* grad) {
     if (!grad) {
         set_last_error("grad result is NULL");
@@ -942,6 +1174,35 @@ tl_status tl_poisson(const float* mean, int32_t n, uint64_t seed, uint32_t step,
     cudaFree(dm);
     cudaFree(dout);
     if (e != cudaSuccess) return cuda_fail(e, "poisson");
+    return TL_OK;
+}
+
+tl_status tl_merge_moments(int32_t n_parts, int32_t L, const int64_t* counts, const double* means,
+                           const double* stddevs, int64_t* count_out, double* mean_out, double* stddev_out) {
+    if (n_parts < 1 || L < 1 || !counts || !means || !stddevs || !count_out || !mean_out || !stddev_out) {
+        set_last_error("bad arguments to tl_merge_moments");
+        return TL_ERR_INVALID_ARGUMENT;
+    }
+    for (int l = 0; l < L; ++l) {
+        double n = 0.0, mean = 0.0, m2 = 0.0;
+        for (int p = 0; p < n_parts; ++p) {
+            const double nb = (double)counts[p];
+            if (nb <= 0) continue;
+            const double mb = means[(size_t)p * L + l];
+            const double sb = stddevs[(size_t)p * L + l];
+            const double m2b = nb > 1 ? sb * sb * (nb - 1.0) : 0.0;
+            const double nn = n + nb;
+            const double d = mb - mean;
+            mean += d * nb / nn;
+            m2 += m2b + d * d * n * nb / nn;
+            n = nn;
+        }
+        mean_out[l] = mean;
+        stddev_out[l] = n > 1 ? sqrt(m2 / (n - 1.0)) : 0.0;
+    }
+    int64_t tot = 0;
+    for (int p = 0; p < n_parts; ++p) tot += counts[p] > 0 ? counts[p] : 0;
+    *count_out = tot;
     return TL_OK;
 }
 

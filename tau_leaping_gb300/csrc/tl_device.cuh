@@ -527,6 +527,25 @@ struct SimParams {
     void* pslots;       // global slots for the plain form
 };
 
+// One item of a batched launch (tl_simulate_batch).
+struct BatchItem {
+    SimParams p;
+    long long unit_begin, units;
+    int lane_mode;  // 1: a unit is 32 realizations, one per lane
+    int stage_off;  // byte offset of the model's tables in the staged region, -1: global
+};
+
+struct BatchParams {
+    const BatchItem* items;
+    int n_items;
+    long long total_units;
+    const unsigned char* stage_src;
+    int stage_bytes;
+    int warp_slot_bytes;
+    int params_bytes;
+    unsigned long long* wctr;
+};
+
 template <class Pop>
 struct Slot {
     Pop* x;
@@ -857,7 +876,7 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
             while (st.kpt <= p.n_int && st.t + dt >= grid_time<TimeT>(p, T, st.kpt))
                 record_point<Grp, Pop>(g, p, s.x, samp, st.kpt++);
             if (st.kpt > p.n_int) {
-                if (SENS) {
+                if (SENS && score) {
                     const float rem = (float)((TimeT)T - st.t);
                     for (int m = g.rank(); m < p.M; m += g.size()) {
                         const float c = __ldg(rate + m);
@@ -869,7 +888,7 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
                 g.sync();
                 return;
             }
-            if (SENS) {
+            if (SENS && score) {
                 const float dtf = (float)dt;
                 for (int m = g.rank(); m < p.M; m += g.size()) {
                     const float c = __ldg(rate + m);
@@ -952,7 +971,7 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
             return;
         }
     }
-    if (SENS) {
+    if (SENS && score) {
         // score_j += (k_j - a_j*tau)/c_j with a_j recomputed from the old state
         const bool cc = flag(f, TL_FLAG_COMPAT_CRIT);
         const float tauf = (float)tau;

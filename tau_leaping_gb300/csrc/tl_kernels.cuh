@@ -135,6 +135,36 @@ struct GroupOf<0> {
     static TL_D int index() { return 0; }
 };
 
+// One realization from x0 to t_final (the body of the persistent loop).
+template <class Grp, class Pop, bool SENS>
+TL_D void run_realization(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& s, long long w,
+                          long long& nl, long long& ns, long long& nr, long long& ntr) {
+    const int P = p.n_int + 1;
+    const int set = (int)(w / p.R);
+    const uint32_t r = (uint32_t)(p.r_off + w - (long long)set * p.R);
+    Pop* samp = reinterpret_cast<Pop*>(p.samples) + (size_t)w * P * p.K;
+    float* score = (SENS && p.scores) ? p.scores + (size_t)w * p.M : nullptr;
+    const Pop* x0 = reinterpret_cast<const Pop*>(p.x0);
+    for (int i = g.rank(); i < p.N; i += g.size()) s.x[i] = x0[i];
+    if (SENS && score)
+        for (int j = g.rank(); j < p.M; j += g.size()) score[j] = 0.f;
+    g.sync();
+    RState<double> st{0.0, 1, 0u, 0, 0, 0, 0, 0};
+    record_point<Grp, Pop>(g, p, s.x, samp, 0);
+    while (!st.done) {
+        do_step<Grp, Pop, double, SENS>(g, p, mv, s, set, r, samp, score, st);
+        if (!st.done && p.max_steps > 0 && st.nsteps >= p.max_steps) {
+            while (st.kpt <= p.n_int) record_point<Grp, Pop>(g, p, s.x, samp, st.kpt++);
+            st.done = 1;
+            ntr++;
+        }
+    }
+    nl += st.leaps;
+    ns += st.ssa;
+    nr += st.rej;
+    g.sync();
+}
+
 // ---------------------------------------------------------------------------
 // Fused persistent kernel.
 // ---------------------------------------------------------------------------
@@ -158,8 +188,6 @@ __global__ void __launch_bounds__(1024) k_fused(SimParams p) {
     const Grp g = GroupOf<KIND>::make(red);
     Slot<Pop> s = carve_slot<Pop>(slots + (size_t)GroupOf<KIND>::index() * p.slot_bytes, p);
     const long long total = p.R * (long long)p.S;
-    const int P = p.n_int + 1;
-    const Pop* x0 = reinterpret_cast<const Pop*>(p.x0);
     long long nl = 0, ns = 0, nr = 0, ntr = 0;
 
     for (;;) {
@@ -167,34 +195,79 @@ __global__ void __launch_bounds__(1024) k_fused(SimParams p) {
         if (g.leader()) w = (long long)atomicAdd(p.ctr + 0, 1ull);
         w = g.bcast(w, 0);
         if (w >= total) break;
-        const int set = (int)(w / p.R);
-        const uint32_t r = (uint32_t)(p.r_off + w - (long long)set * p.R);
-        Pop* samp = reinterpret_cast<Pop*>(p.samples) + (size_t)w * P * p.K;
-        float* score = SENS ? p.scores + (size_t)w * p.M : nullptr;
-        for (int i = g.rank(); i < p.N; i += g.size()) s.x[i] = x0[i];
-        if (SENS)
-            for (int j = g.rank(); j < p.M; j += g.size()) score[j] = 0.f;
-        g.sync();
-        RState<double> st{0.0, 1, 0u, 0, 0, 0, 0, 0};
-        record_point<Grp, Pop>(g, p, s.x, samp, 0);
-        while (!st.done) {
-            do_step<Grp, Pop, double, SENS>(g, p, mv, s, set, r, samp, score, st);
-            if (!st.done && p.max_steps > 0 && st.nsteps >= p.max_steps) {
-                while (st.kpt <= p.n_int) record_point<Grp, Pop>(g, p, s.x, samp, st.kpt++);
-                st.done = 1;
-                ntr++;
-            }
-        }
-        nl += st.leaps;
-        ns += st.ssa;
-        nr += st.rej;
-        g.sync();
+        run_realization<Grp, Pop, SENS>(g, p, mv, s, w, nl, ns, nr, ntr);
     }
     if (g.leader()) {
         if (nl) atomicAdd(p.ctr + 1, (unsigned long long)nl);
         if (ns) atomicAdd(p.ctr + 2, (unsigned long long)ns);
         if (nr) atomicAdd(p.ctr + 3, (unsigned long long)nr);
         if (ntr) atomicAdd(p.ctr + 4, (unsigned long long)ntr);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Batched persistent kernel: items of several models / configurations.
+// ---------------------------------------------------------------------------
+TL_D void add_counts(unsigned long long* ctr, long long nl, long long ns, long long nr, long long ntr) {
+    if (nl) atomicAdd(ctr + 1, (unsigned long long)nl);
+    if (ns) atomicAdd(ctr + 2, (unsigned long long)ns);
+    if (nr) atomicAdd(ctr + 3, (unsigned long long)nr);
+    if (ntr) atomicAdd(ctr + 4, (unsigned long long)ntr);
+}
+
+template <class Pop, bool SENS>
+__global__ void __launch_bounds__(256) k_batch(BatchParams bp) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ __align__(8) unsigned long long mbar;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (bp.stage_bytes > 0) {
+        SimParams sp0{};
+        sp0.blob = bp.stage_src;
+        sp0.stage_bytes = bp.stage_bytes;
+        if (!stage_blob(smem, sp0, &mbar)) {
+            if (threadIdx.x == 0) atomicOr((unsigned*)(bp.items[0].p.ctr + 5), kErrWaitTimeout | kErrStage);
+            return;
+        }
+    }
+    unsigned char* wslot = smem + bp.stage_bytes + (size_t)warp * bp.warp_slot_bytes;
+    SimParams* sp = reinterpret_cast<SimParams*>(smem + bp.stage_bytes + (size_t)nw * bp.warp_slot_bytes +
+                                                 (size_t)warp * bp.params_bytes);
+    int cur = -1;
+    for (;;) {
+        long long u = 0;
+        if (lane == 0) u = (long long)atomicAdd(bp.wctr, 1ull);
+        u = __shfl_sync(0xffffffffu, u, 0);
+        if (u >= bp.total_units) break;
+        int it = 0;
+        while (it + 1 < bp.n_items && u >= bp.items[it + 1].unit_begin) ++it;
+        if (it != cur) {
+            __syncwarp();
+            const int* src = reinterpret_cast<const int*>(&bp.items[it].p);
+            int* dst = reinterpret_cast<int*>(sp);
+            for (int k = lane; k < (int)(sizeof(SimParams) / 4); k += 32) dst[k] = src[k];
+            __syncwarp();
+            cur = it;
+        }
+        const SimParams& p = *sp;
+        const int soff = bp.items[it].stage_off;
+        const MView mv = soff >= 0 ? staged_view(smem + soff, p) : p.g;
+        const long long local = u - bp.items[it].unit_begin;
+        long long a = 0, b = 0, c = 0, d = 0;
+        if (!bp.items[it].lane_mode) {
+            const GWarp g{lane};
+            Slot<Pop> s = carve_slot<Pop>(wslot, p);
+            run_realization<GWarp, Pop, SENS>(g, p, mv, s, local, a, b, c, d);
+            if (lane == 0) add_counts(p.ctr, a, b, c, d);  // state is replicated across the warp
+        } else {
+            const long long wi = local * 32 + lane;
+            if (wi < p.R * (long long)p.S) {
+                const G1 g{};
+                Slot<Pop> s = carve_slot<Pop>(wslot + (size_t)lane * p.slot_bytes, p);
+                run_realization<G1, Pop, SENS>(g, p, mv, s, wi, a, b, c, d);
+                add_counts(p.ctr, a, b, c, d);
+            }
+        }
+        __syncwarp();
     }
 }
 

@@ -14,6 +14,11 @@ cudaError_t launch_fused(const SimParams& p, int kind, bool sens, int block, int
                          cudaStream_t st);
 template <class Pop>
 cudaError_t fused_occupancy(int kind, bool sens, int block, size_t smem, int* blocks_per_sm);
+struct BatchParams;
+template <class Pop>
+cudaError_t launch_batch(const BatchParams& bp, bool sens, int block, int grid, size_t smem, cudaStream_t st);
+template <class Pop>
+cudaError_t batch_occupancy(bool sens, int block, size_t smem, int* blocks_per_sm);
 template <class Pop>
 cudaError_t launch_plain_init(const SimParams& p, cudaStream_t st);
 template <class Pop>

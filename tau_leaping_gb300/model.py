@@ -248,3 +248,52 @@ def poisson(mean, seed: int = 1, step: int = 0, compat: bool = False) -> np.ndar
     F.check(F.lib().tl_poisson(_ptr(mean, C.c_float), len(mean), seed, step, int(compat), _ptr(out, C.c_int32)),
             "tl_poisson")
     return out
+
+
+def simulate_batch(items: list[dict], stream=None) -> list[dict]:
+    """One launch over several (model, configuration) items (tl_simulate_batch).
+
+    Each item: dict(model=Model, t_final=..., n=..., seed=..., tracked=[...],
+    intervals=1, rate_sets=None, t_final_sets=None, sensitivity=False,
+    keep_samples=False, flags=0, eps=0.03, realization_offset=0).
+    Returns per item a dict with mean / stddev / times (and grad, stderr,
+    mean_final with sensitivity, samples with keep_samples) plus counters.
+    """
+    keep, arr = [], (F.BatchItem * len(items))()
+    outs = []
+    for k, it in enumerate(items):
+        m: Model = it["model"]
+        tracked = [m.species_index(t) if isinstance(t, str) else int(t) for t in it["tracked"]]
+        intervals = int(it.get("intervals", 1))
+        flags = int(it.get("flags", 0)) | (F.FLAG_KEEP_SAMPLES if it.get("keep_samples") else 0)
+        cfg, kp = m._cfg(it["t_final"], it["n"], it.get("seed", 1), intervals, tracked, it.get("eps", 0.03), 0, flags,
+                         it.get("rate_sets"), it.get("t_final_sets"), it.get("max_steps", 0), 0, None,
+                         realization_offset=it.get("realization_offset", 0))
+        S, Pn, K, M = max(1, cfg.n_rate_sets), intervals + 1, len(tracked), m.n_channels
+        o = {"times": np.zeros((S, Pn)), "mean": np.zeros((S, Pn, K)), "stddev": np.zeros((S, Pn, K))}
+        if it.get("keep_samples"):
+            o["samples"] = np.zeros((S, it["n"], Pn, K), np.int64)
+        res = F.Result()
+        res.times, res.mean, res.stddev = _ptr(o["times"], C.c_double), _ptr(o["mean"], C.c_double), \
+            _ptr(o["stddev"], C.c_double)
+        res.samples = _ptr(o.get("samples"), C.c_int64)
+        gr = None
+        if it.get("sensitivity"):
+            o["grad"], o["stderr"], o["mean_final"] = np.zeros((S, K, M)), np.zeros((S, K, M)), np.zeros((S, K))
+            gr = F.GradResult(_ptr(o["grad"], C.c_double), _ptr(o["stderr"], C.c_double),
+                              _ptr(o["mean_final"], C.c_double))
+        arr[k].model = m._h
+        arr[k].cfg = C.pointer(cfg)
+        arr[k].result = C.pointer(res)
+        arr[k].grad = C.pointer(gr) if gr is not None else None
+        keep += [cfg, kp, res, gr]
+        outs.append((o, res))
+    F.check(F.lib().tl_simulate_batch(arr, len(items), stream), "tl_simulate_batch")
+    out = []
+    for o, res in outs:
+        o.update(leaps=res.leaps, ssa_steps=res.ssa_steps, rejections=res.rejections, truncated=res.truncated,
+                 kernel_ms=res.kernel_ms, variant=res.variant_used, grid=res.grid_used,
+                 block_threads=res.block_threads_used)
+        out.append(o)
+    del keep
+    return out
