@@ -157,7 +157,12 @@ enum tl_variant {
 /* Behaviour flags. */
 #define TL_FLAG_SENSITIVITY (1u << 0)   /* accumulate likelihood-ratio scores */
 #define TL_FLAG_KEEP_SAMPLES (1u << 1)  /* return per-realization samples    */
-#define TL_FLAG_AUTOTUNE_MEASURE (1u << 2) /* AUTO: time candidate variants  */
+#define TL_FLAG_AUTOTUNE_MEASURE (1u << 2) /* AUTO: time candidate plans on a
+                                             prefix of the ensemble, cache
+                                             the fastest in the model       */
+#define TL_FLAG_NO_STAGE (1u << 3)       /* read model tables through L1/L2
+                                            instead of staging them in
+                                            shared memory (tuning knob)     */
 /* Reference-compatibility switches (each reproduces one behaviour of the
  * shipped reference; default off = Cao-Gillespie-Petzold 2006 semantics). */
 #define TL_FLAG_COMPAT_G (1u << 8)       /* g read from channel order at the

@@ -176,30 +176,44 @@ struct Plan {
     size_t smem = 0;
     int stage = 0;      // staged bytes (0 = constants read through L1/L2)
     int variant = TL_VARIANT_WARP;
+    bool row_warp = false;
 };
 
 // Autotuner, heuristic part: the group width follows the model size.
 //  * a handful of channels: one realization per thread (all lanes busy on
-//    independent realizations);
-//  * up to a few thousand channels: one warp per realization, per-warp state
-//    and propensities in shared memory;
-//  * larger: one CTA per realization (propensities of ~30k channels fill
-//    most of the 227 KB of shared memory).
+//    independent realizations); small ensembles use small blocks so that
+//    every SM gets work;
+//  * per-realization state up to 8 KB: one warp per realization, 256-thread
+//    blocks, model tables staged in shared memory;
+//  * up to 64 KB: one 128-thread CTA per realization, tables through L1/L2,
+//    so that 16 CTAs fit an SM (chain-sized models);
+//  * larger: one 512-thread CTA per realization (propensities of ~30k
+//    channels fill most of the 227 KB of shared memory).
+static int heuristic_variant(const tl_model* m, size_t sb) {
+    if (m->h.M <= 16 && m->h.N <= 16) return TL_VARIANT_THREAD;
+    if (sb <= 8 * 1024) return TL_VARIANT_WARP;
+    return TL_VARIANT_CTA;
+}
+
 static tl_status make_plan(const tl_model* m, int variant, int block_req, bool sens, bool compat_stoich,
-                           long long total, Plan& pl) {
+                           bool no_stage, long long total, Plan& pl) {
     const size_t sb = slot_bytes(m);
     const int smax = max_smem_optin() - 2048;
-    const int stage = compat_stoich ? 0 : m->d.stage_bytes;
-    if (variant == TL_VARIANT_AUTO) {
-        if (m->h.M <= 16 && m->h.N <= 16) variant = TL_VARIANT_THREAD;
-        else if (sb * 4 + (size_t)stage <= (size_t)smax || sb * 4 <= (size_t)smax) variant = TL_VARIANT_WARP;
-        else variant = TL_VARIANT_CTA;
-    }
+    const int stage = (compat_stoich || no_stage) ? 0 : m->d.stage_bytes;
+    const bool autov = variant == TL_VARIANT_AUTO;
+    if (autov) variant = heuristic_variant(m, sb);
     pl.variant = variant;
     int groups_per_block = 1;
+    const int nsm = sm_count();
     if (variant == TL_VARIANT_THREAD) {
         pl.kind = 1;
-        pl.block = block_req > 0 ? block_req : 128;
+        int b = block_req;
+        if (b <= 0) {
+            // spread small ensembles over every SM
+            const long long per_sm = (total + nsm - 1) / nsm;
+            b = (int)std::min<long long>(128, std::max<long long>(32, (per_sm + 31) / 32 * 32));
+        }
+        pl.block = b;
         groups_per_block = pl.block;
     } else if (variant == TL_VARIANT_WARP) {
         pl.kind = 32;
@@ -207,7 +221,7 @@ static tl_status make_plan(const tl_model* m, int variant, int block_req, bool s
         groups_per_block = pl.block / 32;
     } else if (variant == TL_VARIANT_CTA) {
         pl.kind = 0;
-        pl.block = block_req > 0 ? block_req : 512;
+        pl.block = block_req > 0 ? block_req : (sb <= 64 * 1024 ? 128 : 512);
         groups_per_block = 1;
     } else {
         set_last_error("unknown variant");
@@ -226,15 +240,22 @@ static tl_status make_plan(const tl_model* m, int variant, int block_req, bool s
         set_last_error("model too large for the shared-memory slot of this variant");
         return TL_ERR_UNSUPPORTED;
     }
-    pl.stage = ((size_t)groups_per_block * sb + (size_t)stage <= (size_t)smax) ? stage : 0;
+    // chain-sized CTA groups leave the tables in L1/L2 (staging them would
+    // cost more shared memory than the realization itself)
+    const bool stage_ok = !(autov && pl.kind == 0 && sb <= 64 * 1024);
+    pl.stage = (stage_ok && (size_t)groups_per_block * sb + (size_t)stage <= (size_t)smax) ? stage : 0;
     pl.smem = (size_t)pl.stage + (size_t)groups_per_block * sb;
+    pl.row_warp = pl.kind == 0 && m->h.max_row > 32;
     int bps = 0;
     cudaError_t e = m->h.pop_bits == 64 ? fused_occupancy<long long>(pl.kind, sens, pl.block, pl.smem, &bps)
                                         : fused_occupancy<int>(pl.kind, sens, pl.block, pl.smem, &bps);
     if (e != cudaSuccess) return cuda_fail(e, "occupancy");
-    if (bps < 1) bps = 1;
+    if (bps < 1) {
+        set_last_error("the launch does not fit an SM");
+        return TL_ERR_UNSUPPORTED;
+    }
     const long long need = (total + groups_per_block - 1) / groups_per_block;
-    pl.grid = (int)std::min<long long>((long long)sm_count() * bps, std::max<long long>(need, 1));
+    pl.grid = (int)std::min<long long>((long long)nsm * bps, std::max<long long>(need, 1));
     return TL_OK;
 }
 
@@ -427,6 +448,7 @@ static tl_status job_bind(Job& J, unsigned char* B, cudaStream_t st) {
     p.off_cp = m->d.off_cp;
     p.off_rv = m->d.off_rv;
     p.slot_bytes = (int)slot_bytes(m);
+    p.row_warp = J.pl.row_warp ? 1 : 0;
     p.ctr = rb.ctr;
     p.pstate = rb.pstate;
     p.pslots = rb.pslots;
@@ -522,6 +544,78 @@ static double ms_since(std::chrono::steady_clock::time_point t0) {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
+// Autotuner, measured part (TL_FLAG_AUTOTUNE_MEASURE): time every plan that
+// fits on the first realizations of this very ensemble (identical streams,
+// so identical work per candidate), keep the fastest in the model handle,
+// keyed by the flags that change the kernel.  The trial writes only the
+// prefix of the sample buffer, which the real run then overwrites.
+static tl_status autotune_measure(Job& J, cudaStream_t st) {
+    tl_model* m = J.m;
+    const unsigned key = 0x80000000u | (J.sens ? 1u : 0u) | (J.compat_stoich ? 2u : 0u) |
+                         (unsigned)(J.cfg->flags & ~(TL_FLAG_KEEP_SAMPLES | TL_FLAG_AUTOTUNE_MEASURE)) << 4;
+    if (m->tuned_key != key) {
+        struct Cand {
+            int variant, block;
+            bool nostage;
+        };
+        std::vector<Cand> cands;
+        if (m->h.M <= 64 && m->h.N <= 64)
+            for (int b : {32, 64, 128}) cands.push_back({TL_VARIANT_THREAD, b, false});
+        for (int b : {64, 128, 256})
+            for (bool ns : {false, true}) cands.push_back({TL_VARIANT_WARP, b, ns});
+        for (int b : {64, 128, 256, 512, 1024})
+            for (bool ns : {false, true}) cands.push_back({TL_VARIANT_CTA, b, ns});
+        const long long trial = std::min<long long>(J.total, 4096);
+        SimParams tp = J.p;
+        tp.R = trial;
+        tp.S = 1;
+        cudaEvent_t e0, e1;
+        TLC(cudaEventCreate(&e0));
+        TLC(cudaEventCreate(&e1));
+        float best = 3.4e38f;
+        Cand win{0, 0, false};
+        for (const Cand& c : cands) {
+            Plan pl;
+            if (make_plan(m, c.variant, c.block, J.sens, J.compat_stoich, c.nostage, trial, pl) != TL_OK) continue;
+            if (c.variant == TL_VARIANT_THREAD && c.block != pl.block) continue;
+            tp.stage_bytes = pl.stage;
+            tp.row_warp = pl.row_warp ? 1 : 0;
+            if (cudaMemsetAsync(tp.ctr, 0, 64, st) != cudaSuccess) break;
+            cudaEventRecord(e0, st);
+            cudaError_t le = J.w == 8 ? launch_fused<long long>(tp, pl.kind, J.sens, pl.block, pl.grid, pl.smem, st)
+                                      : launch_fused<int>(tp, pl.kind, J.sens, pl.block, pl.grid, pl.smem, st);
+            cudaEventRecord(e1, st);
+            if (le != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+                cudaGetLastError();
+                continue;
+            }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) {
+                best = ms;
+                win = c;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        TLC(cudaMemsetAsync(J.p.ctr, 0, 64, st));
+        if (win.variant == 0) {
+            set_last_error("autotuner found no plan that fits");
+            return TL_ERR_UNSUPPORTED;
+        }
+        m->tuned_key = key;
+        m->tuned_variant = win.variant;
+        m->tuned_block = win.block;
+        m->tuned_nostage = win.nostage ? 1 : 0;
+    }
+    tl_status ps = make_plan(m, m->tuned_variant, m->tuned_block, J.sens, J.compat_stoich, m->tuned_nostage != 0,
+                             J.total, J.pl);
+    if (ps != TL_OK) return ps;
+    J.p.stage_bytes = J.pl.stage;
+    J.p.row_warp = J.pl.row_warp ? 1 : 0;
+    return TL_OK;
+}
+
 static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad_result* grad) {
     const auto t0 = std::chrono::steady_clock::now();
     Job J;
@@ -533,8 +627,10 @@ static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad
     if (ps != TL_OK) return ps;
     TLC(cudaSetDevice(m->d.device));
     cudaStream_t st = (cudaStream_t)cfg->stream;
+    const bool no_stage = (cfg->flags & TL_FLAG_NO_STAGE) != 0;
+    const bool measure = !J.plain && cfg->variant == TL_VARIANT_AUTO && (cfg->flags & TL_FLAG_AUTOTUNE_MEASURE);
     if (!J.plain) {
-        ps = make_plan(m, cfg->variant, cfg->block_threads, J.sens, J.compat_stoich, J.total, J.pl);
+        ps = make_plan(m, cfg->variant, cfg->block_threads, J.sens, J.compat_stoich, no_stage, J.total, J.pl);
         if (ps != TL_OK) return ps;
     } else {
         J.pl.variant = TL_VARIANT_PLAIN;
@@ -549,6 +645,10 @@ static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad
     if (ps != TL_OK) return ps;
     ps = job_bind(J, reinterpret_cast<unsigned char*>(base), st);
     if (ps != TL_OK) return ps;
+    if (measure) {
+        ps = autotune_measure(J, st);
+        if (ps != TL_OK) return ps;
+    }
     const SimParams& p = J.p;
     const size_t w = J.w;
 

@@ -266,23 +266,18 @@ TL_D int poisson_reference(float mu, Rng& rng) {
 template <class Pop>
 TL_D void propensity(const int4 ch, float c, const Pop* x, int nc, bool compat_crit, float& a,
                      bool& crit) {
+    // Branch-free over the order so that a warp's mixed-order channels do
+    // not diverge.  For order 1/3 the table holds s1 = s0 (order 0: s0 = s1
+    // = 0), so both loads are always in bounds.  The products keep the
+    // reference's evaluation order: (c*x0)*x1, and (c*x0)*(x0-1)/2 with the
+    // halving exact.
     const int order = ch.z;
-    if (order == 1) {
-        const Pop x0 = x[ch.x];
-        a = c * (float)x0;
-        crit = x0 < (Pop)nc;
-    } else if (order == 2) {
-        const Pop x0 = x[ch.x], x1 = x[ch.y];
-        a = c * (float)x0 * (float)x1;
-        crit = x0 < (Pop)nc || x1 < (Pop)nc;
-    } else if (order == 3) {
-        const Pop x0 = x[ch.x];
-        a = c * (float)x0 * (float)(x0 - 1) * 0.5f;
-        crit = compat_crit ? (x0 * 2 < (Pop)nc) : (x0 < (Pop)(2 * nc));
-    } else {
-        a = c;
-        crit = false;
-    }
+    const Pop x0 = x[ch.x], x1 = x[ch.y];
+    const float f0 = order == 0 ? 1.f : (float)x0;
+    const float f1 = order == 2 ? (float)x1 : order == 3 ? (float)(x0 - 1) * 0.5f : 1.f;
+    a = c * f0 * f1;
+    const Pop t0 = order == 3 ? (compat_crit ? (Pop)((nc + 1) / 2) : (Pop)(2 * nc)) : (Pop)nc;
+    crit = order != 0 && (x0 < t0 || (order == 2 && x1 < (Pop)nc));
 }
 
 // g_i of the CGP bound.  kind: 0 not a reactant, 1 HOR 1, 2 HOR 2 (S_i+S_k),
@@ -520,6 +515,7 @@ struct SimParams {
     int stage_bytes;    // 0 = no staging
     int off_chan, off_gkind, off_perm, off_rp, off_vc, off_cp, off_rv;  // byte offsets (net)
     int slot_bytes;     // per group
+    int row_warp;       // CTA groups: one warp per species row (long rows)
     unsigned long long* ctr; // [0] work, [1] leaps, [2] ssa, [3] rejections,
                              // [4] truncated, [5] error bits, [6] done count
     // plain form state
@@ -618,13 +614,17 @@ TL_D float pass_tau(const Grp& g, const SimParams& p, const MView& mv, const Pop
                     float* mu_out, float* s2_out) {
     const bool all_rows = flag(p.flags, TL_FLAG_COMPAT_STOICH);
     float tmin = kInfF;
+    bool done = false;
     if constexpr (Grp::kWidth == 0) {
+      if (p.row_warp) {
         // one warp per species row, lanes stride the row's entries
-        for (int i = g.warp; i < p.N; i += g.nwarps) {
+        const GCta& gc = g;
+        done = true;
+        for (int i = gc.warp; i < p.N; i += gc.nwarps) {
             if (!all_rows && mv.gkind[i] == 0 && !OUT) continue;
             float mu = 0.f, s2 = 0.f;
             const int e = mv.rp[i + 1];
-            for (int q = mv.rp[i] + g.lane; q < e; q += 32) {
+            for (int q = mv.rp[i] + gc.lane; q < e; q += 32) {
                 const int pk = mv.vc[q];
                 const float aj = a[unpack_idx(pk)];
                 if (!is_crit(aj)) {
@@ -639,7 +639,7 @@ TL_D float pass_tau(const Grp& g, const SimParams& p, const MView& mv, const Pop
                 mu += __shfl_xor_sync(0xffffffffu, mu, o);
                 s2 += __shfl_xor_sync(0xffffffffu, s2, o);
             }
-            if (g.lane == 0) {
+            if (gc.lane == 0) {
                 if (OUT) {
                     mu_out[i] = mu;
                     s2_out[i] = s2;
@@ -647,7 +647,9 @@ TL_D float pass_tau(const Grp& g, const SimParams& p, const MView& mv, const Pop
                 if (all_rows || mv.gkind[i] != 0) tmin = fminf(tmin, species_bound<Pop>(p, mv, x, a, i, mu, s2));
             }
         }
-    } else {
+      }
+    }
+    if (!done) {
         for (int ii = g.rank(); ii < p.N; ii += g.size()) {
             const int i = mv.perm[ii];
             if (!all_rows && mv.gkind[i] == 0 && !OUT) continue;
@@ -679,24 +681,30 @@ template <class Grp, class Pop>
 TL_D bool pass_update(const Grp& g, const SimParams& p, const MView& mv, const Pop* x, const int* k,
                       Pop* xn, bool& ovf) {
     bool neg = false, of = false;
+    bool done = false;
     if constexpr (Grp::kWidth == 0) {
-        for (int i = g.warp; i < p.N; i += g.nwarps) {
+      if (p.row_warp) {
+        const GCta& gc = g;
+        done = true;
+        for (int i = gc.warp; i < p.N; i += gc.nwarps) {
             long long d = 0;
             const int e = mv.urp[i + 1];
-            for (int q = mv.urp[i] + g.lane; q < e; q += 32) {
+            for (int q = mv.urp[i] + gc.lane; q < e; q += 32) {
                 const int pk = mv.uvc[q];
                 d += (long long)unpack_v(pk) * (long long)k[unpack_idx(pk)];
             }
 #pragma unroll
             for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-            if (g.lane == 0) {
+            if (gc.lane == 0) {
                 const long long nx = (long long)x[i] + d;
                 if (sizeof(Pop) == 4 && nx > 2147483647LL) of = true;
                 xn[i] = (Pop)nx;
                 neg |= nx < 0;
             }
         }
-    } else {
+      }
+    }
+    if (!done) {
         for (int ii = g.rank(); ii < p.N; ii += g.size()) {
             const int i = mv.perm[ii];
             long long d = 0;
@@ -918,8 +926,9 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
     TimeT tau;
     bool clamp;
     for (int attempt = 0;; ++attempt) {
-        const U4 w = step_words(p.k0, p.k1, st.step, r, (uint32_t)set);
         const float a0cf = g.sumf(pac);
+        // the step's scalar words are needed only when a channel is critical
+        const U4 w = a0cf > 0.f ? step_words(p.k0, p.k1, st.step, r, (uint32_t)set) : U4{0u, 0u, 0u, 0u};
         int jc = -1;
         float tau2 = kInfF;
         if (a0cf > 0.f) {

@@ -37,6 +37,7 @@ struct HostModel {
     std::vector<int32_t> rowperm;          // species rows by net length, longest first
     std::vector<std::string> names;
     int max_order = 0;
+    int max_row = 0;  // longest net species row
 };
 
 // Build every derived table from the raw channel-major entries in `h`
@@ -81,5 +82,7 @@ struct tl_model {
     // scratch (grow-only)
     void* scratch = nullptr;
     size_t scratch_bytes = 0;
-    int tuned_variant = 0, tuned_block = 0;
+    // measured autotuner cache (TL_FLAG_AUTOTUNE_MEASURE)
+    int tuned_variant = 0, tuned_block = 0, tuned_nostage = 0;
+    unsigned tuned_key = 0;
 };

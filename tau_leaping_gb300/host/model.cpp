@@ -215,6 +215,8 @@ tl_status derive_tables(HostModel& h, std::string& err) {
     h.net_rv.resize(nrows.size());
     for (size_t q = 0; q < nrows.size(); ++q) h.net_rv[q] = pack(nrows[q], nvals[q]);
     to_rows(N, M, h.net_cp, nrows, nvals, h.net_rp, h.net_vc);
+    h.max_row = 0;
+    for (int i = 0; i < N; ++i) h.max_row = std::max(h.max_row, h.net_rp[(size_t)i + 1] - h.net_rp[(size_t)i]);
     // processing order of species rows: longest first, so the rows a warp
     // walks side by side have similar lengths
     h.rowperm.resize((size_t)N);

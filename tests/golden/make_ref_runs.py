@@ -28,15 +28,19 @@ sys.path.insert(0, str(ROOT))
 REFERENCE = Path("/root/reference")
 
 RUNS = {
-    # name: (model source, t_final, realizations, intervals, tracked names)
-    "test_128": ("examples/test_128.xml", 0.1, 400, 4, ["S1", "S5"]),
-    "chain64": ("chain64", 1.0, 2000, 4, ["S1", "S2", "S33"]),
+    # name: (model source, t_final, realizations, intervals, eps, tracked names)
+    # The reference interpolates linearly between the states it logs before
+    # each step; the chain takes only ~17 leaps at eps 0.03, so it runs at
+    # eps 0.003 (tenfold finer leaps) to keep that interpolation far below
+    # the sampling error.
+    "test_128": ("examples/test_128.xml", 0.1, 400, 4, 0.03, ["S1", "S5"]),
+    "chain64": ("chain64", 1.0, 2000, 4, 0.003, ["S1", "S2", "S33"]),
 }
 
 
-def run(name, model_path, T, n, intervals, tracked):
+def run(name, model_path, T, n, intervals, eps, tracked):
     exe = ROOT / "oracle" / "_ref" / "ref_driver"
-    out = subprocess.run([str(exe), str(model_path), str(T), str(n), str(intervals), "0.03", "1", *tracked],
+    out = subprocess.run([str(exe), str(model_path), str(T), str(n), str(intervals), str(eps), "1", *tracked],
                          capture_output=True, text=True, check=True, cwd=tempfile.gettempdir()).stdout
     times, blocks, cur, secs, steps = [], [], None, 0.0, 0
     for line in out.splitlines():
@@ -59,7 +63,7 @@ def main():
     build.build()
     out = {}
     with tempfile.TemporaryDirectory() as td:
-        for name, (src, T, n, intervals, tracked) in RUNS.items():
+        for name, (src, T, n, intervals, eps, tracked) in RUNS.items():
             if src.endswith(".xml"):
                 path = REFERENCE / src
             else:
@@ -67,12 +71,13 @@ def main():
                 Model.generate("chain", n_species=64).write_stochkit(path)
             m = Model.from_stochkit(path)
             d = m.desc()
-            times, samples, secs, steps = run(name, path, T, n, intervals, tracked)
+            times, samples, secs, steps = run(name, path, T, n, intervals, eps, tracked)
             idx = np.array([m.species_index(t) for t in tracked], np.int32)
             out.update({f"{name}/{k}": v for k, v in d.items()})
             out.update({f"{name}/times": times, f"{name}/samples": samples.astype(np.float32),
                         f"{name}/tracked": idx, f"{name}/t_final": np.float64(T),
-                        f"{name}/intervals": np.int32(intervals), f"{name}/ref_seconds": np.float64(secs),
+                        f"{name}/intervals": np.int32(intervals), f"{name}/eps": np.float64(eps),
+                        f"{name}/ref_seconds": np.float64(secs),
                         f"{name}/ref_logged_steps": np.int64(steps)})
             print(name, "grid", times, "samples", samples.shape, f"{secs:.1f}s")
     dst = Path(__file__).resolve().parent / "ref_runs.npz"

@@ -10,8 +10,10 @@ and distribution of every tracked species at every grid time must agree at
 
 The reference evaluates the grid by linear interpolation between the states
 it logs before each step; the engine ends a leap exactly on each grid time.
-With thousands of small leaps per realization the difference is far below
-the sampling error of these ensembles.
+Interpolation between states one leap apart lowers the variance, so the
+fixtures use many small leaps per grid interval (test_128 at eps 0.03,
+the chain at eps 0.003), where the difference is far below the sampling
+error of these ensembles.
 """
 from pathlib import Path
 
@@ -50,7 +52,7 @@ def test_compat_mode_matches_reference_run(name):
     m, d = load(name)
     T, P = float(d["t_final"]), int(d["intervals"])
     r = m.simulate(T, 20000, seed=21, intervals=P, tracked=d["tracked"], flags=_ffi.FLAG_COMPAT_REFERENCE,
-                   keep_samples=True)
+                   keep_samples=True, eps=float(d["eps"]))
     ref = d["samples"]                      # [grid, n, K], grid t_k = k*T/P, k < P
     assert np.allclose(d["times"], r.times[0][: len(d["times"])], atol=1e-6)
     for k in range(1, ref.shape[0]):
@@ -63,7 +65,7 @@ def test_default_mode_matches_reference_run_on_chain():
     steps), so the default CGP mode must agree with the reference's run."""
     m, d = load("chain64")
     T, P = float(d["t_final"]), int(d["intervals"])
-    r = m.simulate(T, 20000, seed=22, intervals=P, tracked=d["tracked"], keep_samples=True)
+    r = m.simulate(T, 20000, seed=22, intervals=P, tracked=d["tracked"], keep_samples=True, eps=float(d["eps"]))
     assert r.ssa_steps == 0
     for k in range(1, d["samples"].shape[0]):
         agree(d["samples"][k], r.samples[0, :, k, :], f"chain64 default t={d['times'][k]:.3g}")

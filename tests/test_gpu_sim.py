@@ -153,3 +153,27 @@ def test_colloid_cta_matches_oracle():
     r = o.simulate(0.01, 1024, seed=7, tracked=[0, 1, 9], threads=8)
     compare_final(g.samples[0, :, -1, :], r["samples"][0, :, -1, :], "colloid cta")
     compare_final(w.samples[0, :, -1, :], r["samples"][0, :, -1, :], "colloid warp")
+
+
+def test_measured_autotuner_picks_a_plan_and_caches_it():
+    m = Model.generate("toy", n_species=32, n_channels=64, seed=4, x0_max=3000)
+    o = ora.OracleModel.from_desc(m.desc())
+    flags = _ffi.FLAG_AUTOTUNE_MEASURE
+    a = m.simulate(0.005, 3000, seed=3, tracked=[0, 1], flags=flags, keep_samples=True)
+    b = m.simulate(0.005, 3000, seed=3, tracked=[0, 1], flags=flags, keep_samples=True)
+    assert a.variant in (_ffi.VARIANT_THREAD, _ffi.VARIANT_WARP, _ffi.VARIANT_CTA)
+    assert (a.variant, a.block_threads) == (b.variant, b.block_threads)
+    assert np.array_equal(a.samples, b.samples)
+    r = o.simulate(0.005, 1500, seed=4, tracked=[0, 1], threads=8)
+    compare_final(a.samples[0, :, -1, :], r["samples"][0, :, -1, :], "autotuned")
+
+
+@pytest.mark.parametrize("variant,block", [(_ffi.VARIANT_CTA, 64), (_ffi.VARIANT_CTA, 128), (_ffi.VARIANT_CTA, 256),
+                                           (_ffi.VARIANT_WARP, 64), (_ffi.VARIANT_THREAD, 32)])
+def test_group_widths_agree_on_chain(variant, block):
+    m = Model.generate("chain", n_species=48)
+    o = ora.OracleModel.from_desc(m.desc())
+    g = m.simulate(0.5, 4096, seed=5, tracked=[0, 7], variant=variant, block_threads=block, keep_samples=True,
+                   flags=_ffi.FLAG_NO_STAGE if block == 128 else 0)
+    r = o.simulate(0.5, 2048, seed=6, tracked=[0, 7], threads=8)
+    compare_final(g.samples[0, :, -1, :], r["samples"][0, :, -1, :], f"chain v{variant} b{block}")
