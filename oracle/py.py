@@ -133,3 +133,30 @@ def poisson(mean, seed=1, step=0, compat=False) -> np.ndarray:
     out = np.zeros(len(mean), np.int64)
     lib().ora_poisson(_p(mean, C.c_double), len(mean), seed, step, int(compat), _p(out, C.c_int64))
     return out
+
+
+def chain_exact_moments(x0, c: float, t: float):
+    """Exact mean and variance of the cyclic chain S_i -> S_(i+1 mod N), rate c
+    (closed, first order: every molecule walks the ring independently and
+    jumps at rate c).  A molecule starting at i is at j at time t with
+    probability q[(j - i) mod N], q[d] = sum_k P(Poisson(c t) = N k + d), so
+    the count at j is a sum of binomials:
+        mean_j = sum_i x0_i q[j-i],  var_j = sum_i x0_i q[j-i] (1 - q[j-i]).
+    FP64, the exact solution of the chemical master equation."""
+    from scipy import stats
+    x0 = np.asarray(x0, np.float64)
+    N = len(x0)
+    lam = c * t
+    kmax = int(lam + 40 * np.sqrt(lam) + 60)
+    pk = stats.poisson.pmf(np.arange(kmax + 1), lam)
+    q = np.zeros(N)
+    np.add.at(q, np.arange(kmax + 1) % N, pk)
+    mean = np.zeros(N)
+    var = np.zeros(N)
+    for d in range(N):
+        if q[d] == 0.0:
+            continue
+        src = np.roll(x0, d)  # src[j] = x0[(j - d) mod N]
+        mean += src * q[d]
+        var += src * q[d] * (1.0 - q[d])
+    return mean, var

@@ -488,6 +488,9 @@ struct MView {
 
 TL_HD int unpack_idx(int p) { return p >> 3; }
 TL_HD int unpack_v(int p) { return (p & 7) - 2; }
+// v as a float without an int-to-float conversion: 2^23 + (p & 7) is exact
+// in FP32 and subtracting 2^23 + 2 leaves (p & 7) - 2.
+TL_D float unpack_vf(int p) { return __int_as_float(0x4B000000 | (p & 7)) - 8388610.f; }
 
 struct SimParams {
     int N, M;
@@ -603,9 +606,10 @@ TL_D float species_bound(const SimParams& p, const MView& mv, const Pop* x, cons
     } else {
         gi = g_of(mv.gkind[i], xi);
     }
-    const float num = fmaxf(p.eps * xi / gi, 1.f);
-    const float b1 = num / fabsf(mu);
-    const float b2 = num * num / fabsf(s2);
+    // __fdividef (2 ulp); a zero moment gives an infinite bound as with IEEE
+    const float num = fmaxf(p.eps * __fdividef(xi, gi), 1.f);
+    const float b1 = mu != 0.f ? __fdividef(num, fabsf(mu)) : kInfF;
+    const float b2 = s2 != 0.f ? __fdividef(num * num, fabsf(s2)) : kInfF;
     return fminf(b1, b2);
 }
 
@@ -626,13 +630,11 @@ TL_D float pass_tau(const Grp& g, const SimParams& p, const MView& mv, const Pop
             const int e = mv.rp[i + 1];
             for (int q = mv.rp[i] + gc.lane; q < e; q += 32) {
                 const int pk = mv.vc[q];
-                const float aj = a[unpack_idx(pk)];
-                if (!is_crit(aj)) {
-                    const float v = (float)unpack_v(pk);
-                    const float t = v * aj;
-                    mu += t;
-                    s2 += v * t;
-                }
+                const float aj = fmaxf(a[unpack_idx(pk)], 0.f);
+                const float v = unpack_vf(pk);
+                const float t = v * aj;
+                mu += t;
+                s2 += v * t;
             }
 #pragma unroll
             for (int o = 16; o; o >>= 1) {
@@ -657,13 +659,12 @@ TL_D float pass_tau(const Grp& g, const SimParams& p, const MView& mv, const Pop
             const int e = mv.rp[i + 1];
             for (int q = mv.rp[i]; q < e; ++q) {
                 const int pk = mv.vc[q];
-                const float aj = a[unpack_idx(pk)];
-                if (!is_crit(aj)) {
-                    const float v = (float)unpack_v(pk);
-                    const float t = v * aj;
-                    mu += t;
-                    s2 += v * t;
-                }
+                // critical channels are stored negative: max(a, 0) drops them
+                const float aj = fmaxf(a[unpack_idx(pk)], 0.f);
+                const float v = unpack_vf(pk);
+                const float t = v * aj;
+                mu += t;
+                s2 += v * t;
             }
             if (OUT) {
                 mu_out[i] = mu;

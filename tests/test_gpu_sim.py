@@ -177,3 +177,22 @@ def test_group_widths_agree_on_chain(variant, block):
                    flags=_ffi.FLAG_NO_STAGE if block == 128 else 0)
     r = o.simulate(0.5, 2048, seed=6, tracked=[0, 7], threads=8)
     compare_final(g.samples[0, :, -1, :], r["samples"][0, :, -1, :], f"chain v{variant} b{block}")
+
+
+def test_chain_1024_full_config_error_vs_exact_solution(capsys):
+    """Cyclic chain, 1024 species, 65536 realizations, t_final 1 (mixed
+    precision: FP32 propensities / tau, FP64 time).  Per-species error of the
+    ensemble mean and variance against the exact CME solution (FP64)."""
+    m = Model.generate("chain")
+    mean, var = ora.chain_exact_moments(m.desc()["x0"], 1.0, 1.0)
+    r = m.simulate(1.0, 65536, seed=11, tracked=list(range(1024)))
+    gm, gv = r.mean[0, -1], r.stddev[0, -1] ** 2
+    rel_m = np.abs(gm - mean) / mean
+    rel_v = np.abs(gv - var) / var
+    se_m = np.sqrt(var / 65536) / mean
+    with capsys.disabled():
+        print(f"\nchain-1024 vs exact CME: mean rel err max {rel_m.max():.2e} rms {np.sqrt((rel_m**2).mean()):.2e} "
+              f"(1 s.e. {se_m.mean():.1e}); variance rel err max {rel_v.max():.2e} "
+              f"rms {np.sqrt((rel_v**2).mean()):.2e}; leaps/realization {r.leaps / 65536:.1f}")
+    assert rel_m.max() < 0.01          # tau-leaping bias at eps = 0.03 plus sampling error
+    assert np.sqrt((rel_v ** 2).mean()) < 0.05

@@ -106,3 +106,14 @@ def test_oracle_poisson_sampler_moments():
         s = ora.poisson(np.full(100_000, mu), seed=3).astype(float)
         assert abs(s.mean() - mu) < 5 * np.sqrt(mu / 1e5)
         assert abs(s.var() - mu) < 5 * np.sqrt((mu + 2 * mu * mu) / 1e5)
+
+
+def test_oracle_ssa_matches_exact_chain_solution():
+    m = Model.generate("chain", n_species=24)
+    o = ora.OracleModel.from_desc(m.desc())
+    mean, var = ora.chain_exact_moments(m.desc()["x0"], 1.0, 0.4)
+    x = o.simulate(0.4, 8000, seed=2, method=1, threads=8)["samples"][0, :, -1, :].astype(float)
+    se = np.sqrt(var / len(x))
+    assert np.all(np.abs(x.mean(0) - mean) <= 4 * se)
+    sev = var * np.sqrt(2.0 / len(x))
+    assert np.all(np.abs(x.var(0, ddof=1) - var) <= 4.5 * sev)
