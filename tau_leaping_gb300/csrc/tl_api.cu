@@ -151,7 +151,7 @@ static MView global_view(const tl_model* m, bool raw_mu, bool raw_update) {
 
 static size_t slot_bytes(const tl_model* m) {
     const size_t w = m->h.pop_bits == 64 ? 8 : 4;
-    return al16((size_t)m->h.N * w) * 2 + al16((size_t)m->h.M * 4);
+    return al16((size_t)m->h.N * w) + al16((size_t)m->h.N * 8) + al16((size_t)m->h.M * 4);
 }
 
 static int max_smem_optin() {
@@ -185,10 +185,12 @@ struct Plan {
 //    every SM gets work;
 //  * per-realization state up to 8 KB: one warp per realization, 256-thread
 //    blocks, model tables staged in shared memory;
-//  * up to 64 KB: one 128-thread CTA per realization, tables through L1/L2,
-//    so that 16 CTAs fit an SM (chain-sized models);
-//  * larger: one 512-thread CTA per realization (propensities of ~30k
+//  * up to 64 KB: one 256-thread CTA per realization, tables through L1/L2
+//    (chain-sized models: 1024 species and channels);
+//  * larger: one 1024-thread CTA per realization (propensities of ~30k
 //    channels fill most of the 227 KB of shared memory).
+// The choices follow a sweep of every (variant, block, staging) plan on the
+// four benchmark models on GB300.
 static int heuristic_variant(const tl_model* m, size_t sb) {
     if (m->h.M <= 16 && m->h.N <= 16) return TL_VARIANT_THREAD;
     if (sb <= 8 * 1024) return TL_VARIANT_WARP;
@@ -221,7 +223,7 @@ static tl_status make_plan(const tl_model* m, int variant, int block_req, bool s
         groups_per_block = pl.block / 32;
     } else if (variant == TL_VARIANT_CTA) {
         pl.kind = 0;
-        pl.block = block_req > 0 ? block_req : (sb <= 64 * 1024 ? 128 : 512);
+        pl.block = block_req > 0 ? block_req : (sb <= 64 * 1024 ? 256 : 1024);
         groups_per_block = 1;
     } else {
         set_last_error("unknown variant");
@@ -384,7 +386,7 @@ static void job_layout(Job& J, Carver& c) {
     J.o_gse = J.sens ? c.take((size_t)J.S * J.K * M * 8) : 0;
     J.o_gm = J.sens ? c.take((size_t)J.S * J.K * 8) : 0;
     J.o_ps = J.plain ? c.take((size_t)J.total * 64) : 0;
-    J.o_pslot = J.plain ? c.take((size_t)J.total * 2 * N * J.w) : 0;
+    J.o_pslot = J.plain ? c.take((size_t)J.total * (al16((size_t)N * J.w) + al16((size_t)N * 8))) : 0;
     J.o_aall = J.plain ? c.take((size_t)J.total * M * 4) : 0;
 }
 
@@ -551,8 +553,12 @@ static double ms_since(std::chrono::steady_clock::time_point t0) {
 // prefix of the sample buffer, which the real run then overwrites.
 static tl_status autotune_measure(Job& J, cudaStream_t st) {
     tl_model* m = J.m;
-    const unsigned key = 0x80000000u | (J.sens ? 1u : 0u) | (J.compat_stoich ? 2u : 0u) |
-                         (unsigned)(J.cfg->flags & ~(TL_FLAG_KEEP_SAMPLES | TL_FLAG_AUTOTUNE_MEASURE)) << 4;
+    // the best plan depends on how many realizations fill the GPU: key the
+    // cache by the ensemble size (power-of-two bucket) as well
+    int bucket = 0;
+    while (bucket < 40 && (1LL << bucket) < J.total) ++bucket;
+    const unsigned key = 0x80000000u | (J.sens ? 1u : 0u) | (J.compat_stoich ? 2u : 0u) | ((unsigned)bucket << 2) |
+                         (unsigned)(J.cfg->flags & ~(TL_FLAG_KEEP_SAMPLES | TL_FLAG_AUTOTUNE_MEASURE)) << 8;
     if (m->tuned_key != key) {
         struct Cand {
             int variant, block;
@@ -565,7 +571,8 @@ static tl_status autotune_measure(Job& J, cudaStream_t st) {
             for (bool ns : {false, true}) cands.push_back({TL_VARIANT_WARP, b, ns});
         for (int b : {64, 128, 256, 512, 1024})
             for (bool ns : {false, true}) cands.push_back({TL_VARIANT_CTA, b, ns});
-        const long long trial = std::min<long long>(J.total, 4096);
+        // a prefix large enough to fill the GPU under every candidate
+        const long long trial = std::min<long long>(J.total, 16384);
         SimParams tp = J.p;
         tp.R = trial;
         tp.S = 1;
@@ -1200,7 +1207,7 @@ tl_status tl_replay(tl_model* m, const int64_t* x0, const int32_t* k, int32_t n_
     }
     TLC(cudaSetDevice(m->d.device));
     const size_t w = h.pop_bits == 64 ? 8 : 4;
-    const size_t smem = al16((size_t)N * w) * 2 + 16;
+    const size_t smem = al16((size_t)N * w) + al16((size_t)N * 8) + 16;
     if (smem > (size_t)max_smem_optin()) {
         set_last_error("model too large for tl_replay");
         return TL_ERR_UNSUPPORTED;
@@ -1307,3 +1314,4 @@ tl_status tl_merge_moments(int32_t n_parts, int32_t L, const int64_t* counts, co
 }
 
 }  // extern "C"
+

@@ -548,7 +548,8 @@ struct BatchParams {
 template <class Pop>
 struct Slot {
     Pop* x;
-    Pop* xn;
+    Pop* xn;   // aux region of N x 8 bytes: the next state (CSR gather update) or,
+               // seen as long long, the increments of the CSC scatter update
     float* a;  // propensity (sign bit = critical); holds int firing counts after the Poisson pass
 };
 
@@ -782,8 +783,8 @@ TL_D void record_point(const Grp& g, const SimParams& p, const Pop* x, Pop* samp
 // ints.  A thread takes four consecutive channels at a time so that they
 // share one Philox block for their first uniforms.
 template <class Grp>
-TL_D void pass_fire(const Grp& g, const SimParams& p, float* a, float tauf, int jc, uint32_t step, uint32_t r,
-                    uint32_t set) {
+TL_D void pass_fire(const Grp& g, const SimParams& p, const MView& mv, float* a, float tauf, int jc, uint32_t step,
+                    uint32_t r, uint32_t set, long long* dx) {
     const bool refs = flag(p.flags, TL_FLAG_COMPAT_POISSON);
     const bool vec = (reinterpret_cast<uintptr_t>(a) & 15) == 0;
     int* kk = reinterpret_cast<int*>(a);
@@ -826,7 +827,38 @@ TL_D void pass_fire(const Grp& g, const SimParams& p, float* a, float tauf, int 
             for (int e = 0; e < 4; ++e)
                 if (j0 + e < p.M) kk[j0 + e] = kv[e];
         }
+        if (dx) {
+            // scatter the fired channels' columns: integer adds, exact in any order
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                if (kv[e] == 0 || j0 + e >= p.M) continue;
+                const int j = j0 + e;
+                const int qe = mv.cp[j + 1];
+                for (int q = mv.cp[j]; q < qe; ++q) {
+                    const int pk = mv.rv[q];
+                    const long long d = (long long)unpack_v(pk) * (long long)kv[e];
+                    if constexpr (Grp::kWidth == 1) {
+                        dx[unpack_idx(pk)] += d;
+                    } else {
+                        atomicAdd(reinterpret_cast<unsigned long long*>(dx + unpack_idx(pk)), (unsigned long long)d);
+                    }
+                }
+            }
+        }
     }
+}
+
+// After a scatter update: any x + dx < 0 (reject) or past int32 (overflow)?
+template <class Grp, class Pop>
+TL_D bool pass_check(const Grp& g, const SimParams& p, const Pop* x, const long long* dx, bool& ovf) {
+    bool neg = false, of = false;
+    for (int i = g.rank(); i < p.N; i += g.size()) {
+        const long long nx = (long long)x[i] + dx[i];
+        if (sizeof(Pop) == 4 && nx > 2147483647LL) of = true;
+        neg |= nx < 0;
+    }
+    ovf = g.any(of);
+    return g.any(neg || of);
 }
 
 // ---------------------------------------------------------------------------
@@ -955,11 +987,20 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
         }
         if (!fire) jc = -1;
         const float tauf = (float)tau;
-        pass_fire<Grp>(g, p, s.a, tauf, jc, st.step, r, (uint32_t)set);
+        // thread and warp groups scatter the fired columns into dx (few
+        // channels fire in most leaps); CTA groups gather per species row
+        constexpr bool kScatter = Grp::kWidth != 0;
+        long long* dx = reinterpret_cast<long long*>(s.xn);
+        if (kScatter) {
+            for (int i = g.rank(); i < p.N; i += g.size()) dx[i] = 0;
+            g.sync();
+        }
+        pass_fire<Grp>(g, p, mv, s.a, tauf, jc, st.step, r, (uint32_t)set, kScatter ? dx : nullptr);
         int* kk = reinterpret_cast<int*>(s.a);
         g.sync();
         bool ovf = false;
-        const bool bad = pass_update<Grp, Pop>(g, p, mv, s.x, kk, s.xn, ovf);
+        const bool bad = kScatter ? pass_check<Grp, Pop>(g, p, s.x, dx, ovf)
+                                  : pass_update<Grp, Pop>(g, p, mv, s.x, kk, s.xn, ovf);
         if (ovf) {
             if (g.leader()) atomicOr((unsigned*)(p.ctr + 5), kErrOverflow);
             st.done = 1;
@@ -997,7 +1038,10 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
         }
     }
     g.sync();
-    {
+    if constexpr (Grp::kWidth != 0) {
+        const long long* dx = reinterpret_cast<const long long*>(s.xn);
+        for (int i = g.rank(); i < p.N; i += g.size()) s.x[i] = (Pop)((long long)s.x[i] + dx[i]);
+    } else {
         Pop* t = s.x;
         s.x = s.xn;
         s.xn = t;

@@ -99,9 +99,10 @@ template <class Pop>
 TL_D Slot<Pop> carve_slot(unsigned char* base, const SimParams& p) {
     Slot<Pop> s;
     const size_t xb = ((size_t)p.N * sizeof(Pop) + 15) & ~(size_t)15;
+    const size_t ab = ((size_t)p.N * 8 + 15) & ~(size_t)15;
     s.x = reinterpret_cast<Pop*>(base);
     s.xn = reinterpret_cast<Pop*>(base + xb);
-    s.a = reinterpret_cast<float*>(base + 2 * xb);
+    s.a = reinterpret_cast<float*>(base + xb + ab);
     return s;
 }
 
@@ -274,6 +275,12 @@ __global__ void __launch_bounds__(256) k_batch(BatchParams bp) {
 // ---------------------------------------------------------------------------
 // Plain form: one thread per realization, one launch per step, FP32 time.
 // ---------------------------------------------------------------------------
+// Bytes of one plain-form realization's x and aux regions in HBM.
+template <class Pop>
+TL_HD size_t plain_slot_bytes(const SimParams& p) {
+    return (((size_t)p.N * sizeof(Pop) + 15) & ~(size_t)15) + (((size_t)p.N * 8 + 15) & ~(size_t)15);
+}
+
 struct PlainState {
     float t;
     int kpt;
@@ -290,7 +297,7 @@ __global__ void k_plain_init(SimParams p) {
     const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= total) return;
     PlainState* ps = reinterpret_cast<PlainState*>(p.pstate) + w;
-    Pop* xs = reinterpret_cast<Pop*>(p.pslots) + (size_t)w * 2 * p.N;
+    Pop* xs = carve_slot<Pop>(reinterpret_cast<unsigned char*>(p.pslots) + (size_t)w * plain_slot_bytes<Pop>(p), p).x;
     const Pop* x0 = reinterpret_cast<const Pop*>(p.x0);
     for (int i = 0; i < p.N; ++i) xs[i] = x0[i];
     PlainState z{};
@@ -309,10 +316,8 @@ __global__ void k_plain_step(SimParams p, float* a_all) {
     PlainState* ps = reinterpret_cast<PlainState*>(p.pstate) + w;
     PlainState q = *ps;
     if (q.done) return;
-    Pop* xs = reinterpret_cast<Pop*>(p.pslots) + (size_t)w * 2 * p.N;
-    Slot<Pop> s;
-    s.x = xs + (q.par ? p.N : 0);
-    s.xn = xs + (q.par ? 0 : p.N);
+    // state and update scratch in HBM: x | aux (one thread scatters, in place)
+    Slot<Pop> s = carve_slot<Pop>(reinterpret_cast<unsigned char*>(p.pslots) + (size_t)w * plain_slot_bytes<Pop>(p), p);
     s.a = a_all + (size_t)w * p.M;
     Pop* const x_before = s.x;
     const int set = (int)(w / p.R);

@@ -64,3 +64,18 @@ def test_rate_set_batch_gradients_per_set():
         fd, fd_se = crn_fd(m, sets[s].copy(), 0, tf[s], 8000, seed=9, tracked=[0])
         lr, lr_se = g["grad"][s, 0, 0], g["stderr"][s, 0, 0]
         assert abs(lr - fd[0]) <= 3 * np.hypot(lr_se, fd_se[0]), (s, lr, fd)
+
+
+def test_lr_gradient_toy_network_channels():
+    """128 x 256 toy network (the batch workload's second model): LR
+    gradients of E[S1(T)] for the channels with the largest estimated
+    effect, against CRN central differences."""
+    m = Model.generate("toy")
+    base = m.desc()["rate"].astype(np.float64)
+    T, R = 0.005, 20000
+    g = m.sensitivity(T, R, seed=4, tracked=[0])
+    order = np.argsort(-np.abs(g["grad"][0, 0]) / np.maximum(g["stderr"][0, 0], 1e-30))
+    for j in list(order[:4]) + [int(order[100]), int(order[200])]:
+        fd, fd_se = crn_fd(m, base, int(j), T, R, seed=12, tracked=[0])
+        lr, lr_se = g["grad"][0, 0, j], g["stderr"][0, 0, j]
+        assert abs(lr - fd[0]) <= 3 * np.hypot(lr_se, fd_se[0]), (j, lr, lr_se, fd[0], fd_se[0])
