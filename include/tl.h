@@ -262,6 +262,41 @@ typedef struct tl_batch_item {
 tl_status tl_simulate_batch(tl_batch_item *items, int32_t n_items,
                             void *stream);
 
+/*
+ * tl_simulate without any device allocation.  No counterpart in the
+ * reference (it allocates per realization with Thrust vectors).
+ *
+ * For callers that cannot call cudaMalloc: code that runs inside a CUDA
+ * graph capture (cudaMalloc is not capturable), code whose GPU memory is
+ * owned by a pool allocator that has already reserved the device, and
+ * latency-bound loops that cannot afford cudaMalloc / cudaFree's implicit
+ * device-wide synchronisation.  The caller passes inputs and outputs as
+ * for tl_simulate; every piece of device scratch of the run (rate and
+ * t_final tables, per-realization grid samples, counters, reduced
+ * statistics) lives in one file-scope device array of
+ * TL_STATIC_SCRATCH_BYTES that every GPU loading libtl.so holds until the
+ * process exits.
+ *  - The model's tables must already be on the device: any earlier
+ *    tl_simulate / tl_eval_leap / tl_replay call on the model uploads them;
+ *    otherwise TL_ERR_INVALID_ARGUMENT.
+ *  - A run whose scratch exceeds TL_STATIC_SCRATCH_BYTES (about
+ *    S*R*(n_intervals+1)*n_tracked*4 bytes for 32-bit populations, plus
+ *    small tables) is rejected with TL_ERR_INVALID_ARGUMENT and a message
+ *    giving both sizes.  The plain form, sensitivities and the measured
+ *    autotuner are not available here (TL_ERR_UNSUPPORTED / ignored).
+ *  - The first call on a device looks up the array's device address
+ *    (cudaGetSymbolAddress) with that device current; make that first call
+ *    before any stream capture.
+ *  - All calls share the one array, which keeps the last call's contents
+ *    (counters are cleared at the start of each call).  Calls that overlap
+ *    on the GPU - from two host threads, or on two streams - race on it.
+ *  - res->kernel_ms is host-timed from launch to completion (no CUDA event
+ *    is created).
+ */
+#define TL_STATIC_SCRATCH_BYTES (16u << 20)
+tl_status tl_simulate_static(tl_model *m, const tl_run_cfg *cfg,
+                             tl_result *res);
+
 /* ------------------------------------------------------------------------ */
 /* Sensitivity ("backward")                                                 */
 /* ------------------------------------------------------------------------ */

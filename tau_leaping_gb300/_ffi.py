@@ -97,6 +97,7 @@ SIGNATURES = {
     "tl_simulate": (c_i32, [c_vp, P(RunCfg), P(Result)]),
     "tl_sensitivity": (c_i32, [c_vp, P(RunCfg), P(Result), P(GradResult)]),
     "tl_simulate_batch": (c_i32, [P(BatchItem), c_i32, c_vp]),
+    "tl_simulate_static": (c_i32, [c_vp, P(RunCfg), P(Result)]),
     "tl_eval_leap": (c_i32, [c_vp, P(c_i64), c_i32, c_dbl, c_u32, c_i32, P(C.c_float), P(C.c_uint8),
                              P(C.c_float), P(C.c_float), P(C.c_float), P(c_dbl)]),
     "tl_replay": (c_i32, [c_vp, P(c_i64), P(c_i32), c_i32, c_i32, P(c_i64)]),

@@ -1315,3 +1315,85 @@ tl_status tl_merge_moments(int32_t n_parts, int32_t L, const int64_t* counts, co
 
 }  // extern "C"
 
+// ---------------------------------------------------------------------------
+// tl_simulate_static: tl_simulate's run with its device scratch in one
+// file-scope array instead of cudaMalloc'ed memory (see include/tl.h for
+// who needs this and the limits).
+// ---------------------------------------------------------------------------
+namespace tl {
+
+// Held by every GPU that loads the library, until the process exits.
+static __device__ __align__(256) unsigned char g_static_scratch[TL_STATIC_SCRATCH_BYTES];
+
+// Device address of g_static_scratch per device ordinal.  In host code the
+// array's name is only a host-side stand-in, never a device address: the
+// address is looked up once per device, with that device current.
+static std::mutex g_static_mu;
+static void* g_static_addr[256];
+
+static tl_status static_scratch_address(int device, void** out) {
+    if (device < 0 || device >= 256) {
+        set_last_error("device ordinal out of range for the static scratch table");
+        return TL_ERR_INVALID_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_addr[device]) {
+        void* ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_static_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(static scratch)");
+        g_static_addr[device] = ptr;
+    }
+    *out = g_static_addr[device];
+    return TL_OK;
+}
+
+}  // namespace tl
+
+extern "C" tl_status tl_simulate_static(tl_model* m, const tl_run_cfg* cfg, tl_result* res) {
+    const auto t0 = std::chrono::steady_clock::now();
+    if (!m || !cfg) {
+        set_last_error("null model or config");
+        return TL_ERR_INVALID_ARGUMENT;
+    }
+    if (!m->d.blob) {
+        set_last_error("the model's tables are not on the device yet; tl_simulate_static never allocates, so run "
+                       "tl_simulate (or tl_eval_leap / tl_replay) on this model once first");
+        return TL_ERR_INVALID_ARGUMENT;
+    }
+    if (cfg->variant == TL_VARIANT_PLAIN) {
+        set_last_error("tl_simulate_static runs the fused variants only");
+        return TL_ERR_UNSUPPORTED;
+    }
+    Job J;
+    J.m = m;
+    J.cfg = cfg;
+    J.res = res;
+    tl_status ps = job_prepare(J);  // the tables are resident: no upload happens
+    if (ps != TL_OK) return ps;
+    TLC(cudaSetDevice(m->d.device));
+    cudaStream_t st = (cudaStream_t)cfg->stream;
+    ps = make_plan(m, cfg->variant, cfg->block_threads, false, J.compat_stoich,
+                   (cfg->flags & TL_FLAG_NO_STAGE) != 0, J.total, J.pl);
+    if (ps != TL_OK) return ps;
+    Carver c;
+    job_layout(J, c);
+    if (c.off > (size_t)TL_STATIC_SCRATCH_BYTES) {
+        set_last_error("this run needs " + std::to_string(c.off) + " bytes of device scratch; tl_simulate_static has " +
+                       std::to_string((size_t)TL_STATIC_SCRATCH_BYTES) +
+                       " (fewer realizations, tracked species or grid points, or use tl_simulate)");
+        return TL_ERR_INVALID_ARGUMENT;
+    }
+    void* base = nullptr;
+    ps = static_scratch_address(m->d.device, &base);
+    if (ps != TL_OK) return ps;
+    ps = job_bind(J, reinterpret_cast<unsigned char*>(base), st);  // clears the counters
+    if (ps != TL_OK) return ps;
+    const auto tk = std::chrono::steady_clock::now();
+    cudaError_t le = J.w == 8 ? launch_fused<long long>(J.p, J.pl.kind, false, J.pl.block, J.pl.grid, J.pl.smem, st)
+                              : launch_fused<int>(J.p, J.pl.kind, false, J.pl.block, J.pl.grid, J.pl.smem, st);
+    if (le != cudaSuccess) return cuda_fail(le, "simulation launch");
+    ps = job_reduce(J, st);
+    if (ps != TL_OK) return ps;
+    TLC(cudaStreamSynchronize(st));
+    return job_finish(J, ms_since(tk), 1, ms_since(t0));
+}

@@ -193,6 +193,30 @@ class Model:
                          res.kernel_ms, res.total_ms, res.variant_used, res.block_threads_used, res.grid_used,
                          res.launches, st)
 
+    def simulate_static(self, t_final: float, n: int, seed: int = 1, intervals: int = 1, tracked=None,
+                        eps: float = 0.03, variant: int = F.VARIANT_AUTO, flags: int = 0, rate_sets=None,
+                        t_final_sets=None, block_threads: int = 0, stream=None) -> SimResult:
+        """tl_simulate_static: the same run as simulate() with no device
+        allocation (scratch in the library's fixed device array).  For
+        callers that cannot call cudaMalloc; the model must already be on the
+        device (any earlier simulate() uploads it)."""
+        if tracked is None:
+            tracked = list(range(self.n_species))
+        tracked = [self.species_index(t) if isinstance(t, str) else int(t) for t in tracked]
+        cfg, keep = self._cfg(t_final, n, seed, intervals, tracked, eps, variant, flags, rate_sets, t_final_sets, 0,
+                              block_threads, stream)
+        S = max(1, cfg.n_rate_sets)
+        Pn, K = intervals + 1, len(tracked)
+        times, mean, sd = np.zeros((S, Pn)), np.zeros((S, Pn, K)), np.zeros((S, Pn, K))
+        res = F.Result()
+        res.times, res.mean, res.stddev = _ptr(times, C.c_double), _ptr(mean, C.c_double), _ptr(sd, C.c_double)
+        st = F.lib().tl_simulate_static(self._h, C.byref(cfg), C.byref(res))
+        F.check(st, "tl_simulate_static")
+        del keep
+        return SimResult(times, mean, sd, None, res.leaps, res.ssa_steps, res.rejections, res.truncated,
+                         res.kernel_ms, res.total_ms, res.variant_used, res.block_threads_used, res.grid_used,
+                         res.launches, st)
+
     def sensitivity(self, t_final: float, n: int, seed: int = 1, tracked=None, eps: float = 0.03,
                     variant: int = F.VARIANT_AUTO, flags: int = 0, rate_sets=None, t_final_sets=None,
                     block_threads: int = 0, **extra) -> dict:

@@ -1,0 +1,47 @@
+"""tl_simulate_static: the no-allocation entry point.
+
+Some callers of this library cannot call cudaMalloc - code running inside a
+CUDA graph capture, code whose GPU memory a pool allocator has already
+reserved, latency-bound loops that cannot take cudaMalloc / cudaFree's
+device-wide synchronisation.  tl_simulate_static runs the same fused
+simulation as tl_simulate with all of its device scratch in one fixed
+file-scope device array.  These tests call it through the C ABI and compare
+it with tl_simulate; they pass alone in a fresh process and after the rest
+of the suite (this file is collected last)."""
+import numpy as np
+import pytest
+
+from tau_leaping_gb300 import Model, _ffi
+
+pytestmark = pytest.mark.gpu
+
+
+def test_static_entry_matches_simulate_on_two_calls_in_a_row():
+    m = Model.generate("toy", n_species=32, n_channels=64, seed=4, x0_max=3000)
+    kw = dict(t_final=0.005, n=4000, seed=3, tracked=[0, 1, 2], intervals=2)
+    ref = m.simulate(**kw)          # uploads the model's tables (allocates)
+    for _ in range(2):               # the second call reuses the shared array
+        got = m.simulate_static(**kw)
+        assert got.status == 0
+        assert np.allclose(got.mean, ref.mean, rtol=1e-12, atol=0)
+        assert np.allclose(got.stddev, ref.stddev, rtol=1e-12, atol=0)
+        assert np.array_equal(got.times, ref.times)
+        assert (got.leaps, got.ssa_steps, got.rejections) == (ref.leaps, ref.ssa_steps, ref.rejections)
+    d = Model.generate("dimer", x0_min=2000, x0_max=2000)
+    dref = d.simulate(1.0, 3000, seed=2, tracked=[0, 1])
+    dgot = d.simulate_static(1.0, 3000, seed=2, tracked=[0, 1])
+    assert np.allclose(dgot.mean, dref.mean, rtol=1e-12, atol=0)
+
+
+def test_static_entry_limits():
+    m = Model.generate("dimer", x0_min=500, x0_max=500)
+    with pytest.raises(_ffi.TLError) as e:      # tables not resident yet
+        m.simulate_static(0.1, 16, tracked=[0])
+    assert e.value.status == 1 and "never allocates" in str(e.value)
+    m.simulate(0.1, 16, tracked=[0])
+    with pytest.raises(_ffi.TLError) as e:      # scratch beyond the fixed array
+        m.simulate_static(0.1, 3_000_000, tracked=[0, 1, 2], intervals=4)
+    assert e.value.status == 1 and "bytes of device scratch" in str(e.value)
+    with pytest.raises(_ffi.TLError) as e:
+        m.simulate_static(0.1, 16, tracked=[0], variant=_ffi.VARIANT_PLAIN)
+    assert e.value.status == 3
