@@ -27,6 +27,8 @@ if not Path(NVCC).exists():
 CXX = os.environ.get("CXX", "g++")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", str(INC)]
+# extra nvcc flags for tuning builds, e.g. TL_NVCC_FLAGS="-DTL_WARP_MINB=3"
+NVFLAGS += os.environ.get("TL_NVCC_FLAGS", "").split()
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I", str(INC)]
 
 LIB = PKG / "libtl.so"

@@ -229,8 +229,9 @@ static tl_status make_plan(const tl_model* m, int variant, int block_req, bool s
         set_last_error("unknown variant");
         return TL_ERR_INVALID_ARGUMENT;
     }
-    if (pl.block % 32 || pl.block < 32 || pl.block > 1024) {
-        set_last_error("block_threads must be a multiple of 32 in [32, 1024]");
+    if (pl.block % 32 || pl.block < 32 || pl.block > (pl.kind == 0 ? 1024 : 256)) {
+        set_last_error("block_threads must be a multiple of 32 in [32, 256] (thread / warp groups) "
+                       "or [32, 1024] (CTA groups)");
         return TL_ERR_INVALID_ARGUMENT;
     }
     // shrink the block until the slots fit

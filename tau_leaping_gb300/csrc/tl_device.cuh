@@ -213,13 +213,8 @@ TL_HD U4 group_words(uint32_t k0, uint32_t k1, uint32_t g, uint32_t step, uint32
 // uniform would quantise it); k >= 1 continues the sequential inversion on
 // u = 1 - q.  mu >= 10 uses PTRS on the private stream.
 template <class Rng>
-TL_D int poisson_first(float mu, uint32_t w, Rng& rng) {
-    if (!(mu > 0.f)) return 0;
+TL_D int poisson_first_tail(float mu, float q, Rng& rng) {
     if (mu >= 10.f) return poisson_ptrs(mu, rng);
-    const float q = ((float)w + 0.5f) * 2.3283064365386963e-10f;
-    // P(K >= 1) = 1 - exp(-mu); Taylor series below 0.01 (error < mu^4/24)
-    const float s0 = mu < 0.01f ? mu * (1.f - mu * (0.5f - mu * (1.f / 6.f))) : -expm1f(-mu);
-    if (q >= s0) return 0;
     const float u = 1.f - q;
     float p = expf(-mu), F = p;
     for (int k = 1; k < 64; ++k) {
@@ -230,6 +225,17 @@ TL_D int poisson_first(float mu, uint32_t w, Rng& rng) {
         F = Fn;
     }
     return poisson_inversion(mu, rng);
+}
+
+template <class Rng>
+TL_D int poisson_first(float mu, uint32_t w, Rng& rng) {
+    if (!(mu > 0.f)) return 0;
+    if (mu >= 10.f) return poisson_ptrs(mu, rng);
+    const float q = ((float)w + 0.5f) * 2.3283064365386963e-10f;
+    // P(K >= 1) = 1 - exp(-mu); Taylor series below 0.01 (error < mu^4/24)
+    const float s0 = mu < 0.01f ? mu * (1.f - mu * (0.5f - mu * (1.f / 6.f))) : -expm1f(-mu);
+    if (q >= s0) return 0;
+    return poisson_first_tail(mu, q, rng);
 }
 
 TL_D uint32_t word_of(const U4& w, int e) { return e == 0 ? w.x : e == 1 ? w.y : e == 2 ? w.z : w.w; }
@@ -257,6 +263,23 @@ TL_D int poisson_reference(float mu, Rng& rng) {
     } while (s >= 1.f && ++it < 64);
     const float z = u * sqrtf(-2.f * logf(s) / s);
     return (int)fabsf(mu + sqrtf(mu) * z);
+}
+
+// The draw of one channel once its k = 0 test has failed (or its mean is
+// >= 10, or the reference's sampler is asked for), out of line: it is the
+// rare path of a leap, and keeping it out of the unrolled channel loop keeps
+// the hot loop small in the instruction cache.
+#ifdef TL_INLINE_RARE
+#define TL_RARE __device__ __forceinline__
+#else
+#define TL_RARE __device__ __noinline__
+#endif
+static TL_RARE int poisson_rare(float mu, float q, uint32_t j, uint32_t step, uint32_t r, uint32_t set,
+                                         uint32_t k0, uint32_t k1, int refs) {
+    ChanRng rng;
+    rng.init(j, step, r, set, k0, k1);
+    if (refs) return poisson_reference(mu, rng);
+    return poisson_first_tail(mu, q, rng);
 }
 
 // ---------------------------------------------------------------------------
@@ -815,9 +838,17 @@ TL_D void pass_fire(const Grp& g, const SimParams& p, const MView& mv, float* a,
                 kv[e] = (j == jc) ? 1 : 0;
             } else {
                 const float mu = av[e] * tauf;
-                ChanRng rng;
-                rng.init((uint32_t)j, step, r, set, p.k0, p.k1);
-                kv[e] = refs ? poisson_reference(mu, rng) : poisson_first(mu, word_of(gw, e), rng);
+                int k = 0;
+                float q = 0.f;
+                bool rare = refs && mu > 0.f;
+                if (!refs && mu > 0.f) {
+                    // hot path: the k = 0 test of poisson_first on the shared word
+                    q = ((float)word_of(gw, e) + 0.5f) * 2.3283064365386963e-10f;
+                    const float s0 = mu < 0.01f ? mu * (1.f - mu * (0.5f - mu * (1.f / 6.f))) : -expm1f(-mu);
+                    rare = mu >= 10.f || q < s0;
+                }
+                if (rare) k = poisson_rare(mu, q, (uint32_t)j, step, r, set, p.k0, p.k1, refs ? 1 : 0);
+                kv[e] = k;
             }
         }
         if (full) {

@@ -169,8 +169,14 @@ TL_D void run_realization(const Grp& g, const SimParams& p, const MView& mv, Slo
 // ---------------------------------------------------------------------------
 // Fused persistent kernel.
 // ---------------------------------------------------------------------------
+// Thread and warp groups launch at most 256 threads per CTA and ask the
+// compiler for TL_WARP_MINB resident CTAs per SM (register budget
+// 65536 / (256 * TL_WARP_MINB) per thread); CTA groups use up to 1024.
+#ifndef TL_WARP_MINB
+#define TL_WARP_MINB 4
+#endif
 template <int KIND, class Pop, bool SENS>
-__global__ void __launch_bounds__(1024) k_fused(SimParams p) {
+__global__ void __launch_bounds__(KIND == 0 ? 1024 : 256, KIND == 0 ? 1 : TL_WARP_MINB) k_fused(SimParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ __align__(8) unsigned long long mbar;
     __shared__ double red[34];
