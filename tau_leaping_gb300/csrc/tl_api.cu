@@ -151,7 +151,7 @@ static MView global_view(const tl_model* m, bool raw_mu, bool raw_update) {
 
 static size_t slot_bytes(const tl_model* m) {
     const size_t w = m->h.pop_bits == 64 ? 8 : 4;
-    return al16((size_t)m->h.N * w) + al16((size_t)m->h.N * 8) + al16((size_t)m->h.M * 4);
+    return al16((size_t)m->h.N * w) * 2 + al16((size_t)m->h.M * 4);
 }
 
 static int max_smem_optin() {
@@ -387,7 +387,7 @@ static void job_layout(Job& J, Carver& c) {
     J.o_gse = J.sens ? c.take((size_t)J.S * J.K * M * 8) : 0;
     J.o_gm = J.sens ? c.take((size_t)J.S * J.K * 8) : 0;
     J.o_ps = J.plain ? c.take((size_t)J.total * 64) : 0;
-    J.o_pslot = J.plain ? c.take((size_t)J.total * (al16((size_t)N * J.w) + al16((size_t)N * 8))) : 0;
+    J.o_pslot = J.plain ? c.take((size_t)J.total * 2 * al16((size_t)N * J.w)) : 0;
     J.o_aall = J.plain ? c.take((size_t)J.total * M * 4) : 0;
 }
 
@@ -1208,7 +1208,7 @@ tl_status tl_replay(tl_model* m, const int64_t* x0, const int32_t* k, int32_t n_
     }
     TLC(cudaSetDevice(m->d.device));
     const size_t w = h.pop_bits == 64 ? 8 : 4;
-    const size_t smem = al16((size_t)N * w) + al16((size_t)N * 8) + 16;
+    const size_t smem = al16((size_t)N * w) * 2 + 16;
     if (smem > (size_t)max_smem_optin()) {
         set_last_error("model too large for tl_replay");
         return TL_ERR_UNSUPPORTED;

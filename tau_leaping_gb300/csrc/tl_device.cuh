@@ -269,17 +269,16 @@ TL_D int poisson_reference(float mu, Rng& rng) {
 // >= 10, or the reference's sampler is asked for), out of line: it is the
 // rare path of a leap, and keeping it out of the unrolled channel loop keeps
 // the hot loop small in the instruction cache.
-#ifdef TL_INLINE_RARE
-#define TL_RARE __device__ __forceinline__
-#else
-#define TL_RARE __device__ __noinline__
-#endif
-static TL_RARE int poisson_rare(float mu, float q, uint32_t j, uint32_t step, uint32_t r, uint32_t set,
-                                         uint32_t k0, uint32_t k1, int refs) {
+TL_D int poisson_rare_inline(float mu, float q, uint32_t j, uint32_t step, uint32_t r, uint32_t set, uint32_t k0,
+                             uint32_t k1, int refs) {
     ChanRng rng;
     rng.init(j, step, r, set, k0, k1);
     if (refs) return poisson_reference(mu, rng);
     return poisson_first_tail(mu, q, rng);
+}
+static __device__ __noinline__ int poisson_rare(float mu, float q, uint32_t j, uint32_t step, uint32_t r,
+                                                uint32_t set, uint32_t k0, uint32_t k1, int refs) {
+    return poisson_rare_inline(mu, q, j, step, r, set, k0, k1, refs);
 }
 
 // ---------------------------------------------------------------------------
@@ -571,8 +570,7 @@ struct BatchParams {
 template <class Pop>
 struct Slot {
     Pop* x;
-    Pop* xn;   // aux region of N x 8 bytes: the next state (CSR gather update) or,
-               // seen as long long, the increments of the CSC scatter update
+    Pop* xn;   // next state of the update
     float* a;  // propensity (sign bit = critical); holds int firing counts after the Poisson pass
 };
 
@@ -754,9 +752,11 @@ TL_D bool pass_update(const Grp& g, const SimParams& p, const MView& mv, const P
 // cumulative sums across lanes are FP64; inside a lane the FP32 partial sum
 // is replayed in the same order it was accumulated, so the lane intervals
 // tile [0, total) exactly as the totals were formed.
+// Out of line: it runs only when a critical channel fires and in
+// direct-method steps, and one copy keeps the leap loop small.
 template <class Grp, class AccT>
-TL_D int select_channel(const Grp& g, const SimParams& p, const float* a, float lane_part, AccT target,
-                        int want_crit) {
+__device__ __noinline__ int select_channel_impl(const Grp g, const int M, const float* a, float lane_part,
+                                                AccT target, int want_crit) {
     const AccT part = (AccT)lane_part;
     AccT excl;
     if constexpr (Grp::kWidth == 1) {
@@ -771,7 +771,7 @@ TL_D int select_channel(const Grp& g, const SimParams& p, const float* a, float 
     if (g.rank() == L) {
         float acc = 0.f;
         int lastpos = -1;
-        for (int j = g.rank(); j < p.M; j += g.size()) {
+        for (int j = g.rank(); j < M; j += g.size()) {
             const float aj = a[j];
             const bool c = is_crit(aj);
             if (want_crit && !c) continue;
@@ -793,6 +793,12 @@ TL_D int select_channel(const Grp& g, const SimParams& p, const float* a, float 
     }
 }
 
+template <class Grp, class AccT>
+TL_D int select_channel(const Grp& g, const SimParams& p, const float* a, float lane_part, AccT target,
+                        int want_crit) {
+    return select_channel_impl<Grp, AccT>(g, p.M, a, lane_part, target, want_crit);
+}
+
 // Lane partial sum of critical propensities in the same order select uses.
 // (pass_props already returns it as pac.)
 
@@ -806,8 +812,8 @@ TL_D void record_point(const Grp& g, const SimParams& p, const Pop* x, Pop* samp
 // ints.  A thread takes four consecutive channels at a time so that they
 // share one Philox block for their first uniforms.
 template <class Grp>
-TL_D void pass_fire(const Grp& g, const SimParams& p, const MView& mv, float* a, float tauf, int jc, uint32_t step,
-                    uint32_t r, uint32_t set, long long* dx) {
+TL_D void pass_fire(const Grp& g, const SimParams& p, float* a, float tauf, int jc, uint32_t step, uint32_t r,
+                    uint32_t set) {
     const bool refs = flag(p.flags, TL_FLAG_COMPAT_POISSON);
     const bool vec = (reinterpret_cast<uintptr_t>(a) & 15) == 0;
     int* kk = reinterpret_cast<int*>(a);
@@ -847,7 +853,14 @@ TL_D void pass_fire(const Grp& g, const SimParams& p, const MView& mv, float* a,
                     const float s0 = mu < 0.01f ? mu * (1.f - mu * (0.5f - mu * (1.f / 6.f))) : -expm1f(-mu);
                     rare = mu >= 10.f || q < s0;
                 }
-                if (rare) k = poisson_rare(mu, q, (uint32_t)j, step, r, set, p.k0, p.k1, refs ? 1 : 0);
+                if (rare) {
+                    // thread groups inline the rare draw (their loop is per
+                    // thread anyway); warp / CTA groups call it out of line
+                    if constexpr (Grp::kWidth == 1)
+                        k = poisson_rare_inline(mu, q, (uint32_t)j, step, r, set, p.k0, p.k1, refs ? 1 : 0);
+                    else
+                        k = poisson_rare(mu, q, (uint32_t)j, step, r, set, p.k0, p.k1, refs ? 1 : 0);
+                }
                 kv[e] = k;
             }
         }
@@ -858,38 +871,7 @@ TL_D void pass_fire(const Grp& g, const SimParams& p, const MView& mv, float* a,
             for (int e = 0; e < 4; ++e)
                 if (j0 + e < p.M) kk[j0 + e] = kv[e];
         }
-        if (dx) {
-            // scatter the fired channels' columns: integer adds, exact in any order
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                if (kv[e] == 0 || j0 + e >= p.M) continue;
-                const int j = j0 + e;
-                const int qe = mv.cp[j + 1];
-                for (int q = mv.cp[j]; q < qe; ++q) {
-                    const int pk = mv.rv[q];
-                    const long long d = (long long)unpack_v(pk) * (long long)kv[e];
-                    if constexpr (Grp::kWidth == 1) {
-                        dx[unpack_idx(pk)] += d;
-                    } else {
-                        atomicAdd(reinterpret_cast<unsigned long long*>(dx + unpack_idx(pk)), (unsigned long long)d);
-                    }
-                }
-            }
-        }
     }
-}
-
-// After a scatter update: any x + dx < 0 (reject) or past int32 (overflow)?
-template <class Grp, class Pop>
-TL_D bool pass_check(const Grp& g, const SimParams& p, const Pop* x, const long long* dx, bool& ovf) {
-    bool neg = false, of = false;
-    for (int i = g.rank(); i < p.N; i += g.size()) {
-        const long long nx = (long long)x[i] + dx[i];
-        if (sizeof(Pop) == 4 && nx > 2147483647LL) of = true;
-        neg |= nx < 0;
-    }
-    ovf = g.any(of);
-    return g.any(neg || of);
 }
 
 // ---------------------------------------------------------------------------
@@ -1018,20 +1000,11 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
         }
         if (!fire) jc = -1;
         const float tauf = (float)tau;
-        // thread and warp groups scatter the fired columns into dx (few
-        // channels fire in most leaps); CTA groups gather per species row
-        constexpr bool kScatter = Grp::kWidth != 0;
-        long long* dx = reinterpret_cast<long long*>(s.xn);
-        if (kScatter) {
-            for (int i = g.rank(); i < p.N; i += g.size()) dx[i] = 0;
-            g.sync();
-        }
-        pass_fire<Grp>(g, p, mv, s.a, tauf, jc, st.step, r, (uint32_t)set, kScatter ? dx : nullptr);
+        pass_fire<Grp>(g, p, s.a, tauf, jc, st.step, r, (uint32_t)set);
         int* kk = reinterpret_cast<int*>(s.a);
         g.sync();
         bool ovf = false;
-        const bool bad = kScatter ? pass_check<Grp, Pop>(g, p, s.x, dx, ovf)
-                                  : pass_update<Grp, Pop>(g, p, mv, s.x, kk, s.xn, ovf);
+        const bool bad = pass_update<Grp, Pop>(g, p, mv, s.x, kk, s.xn, ovf);
         if (ovf) {
             if (g.leader()) atomicOr((unsigned*)(p.ctr + 5), kErrOverflow);
             st.done = 1;
@@ -1069,10 +1042,7 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
         }
     }
     g.sync();
-    if constexpr (Grp::kWidth != 0) {
-        const long long* dx = reinterpret_cast<const long long*>(s.xn);
-        for (int i = g.rank(); i < p.N; i += g.size()) s.x[i] = (Pop)((long long)s.x[i] + dx[i]);
-    } else {
+    {
         Pop* t = s.x;
         s.x = s.xn;
         s.xn = t;

@@ -99,10 +99,9 @@ template <class Pop>
 TL_D Slot<Pop> carve_slot(unsigned char* base, const SimParams& p) {
     Slot<Pop> s;
     const size_t xb = ((size_t)p.N * sizeof(Pop) + 15) & ~(size_t)15;
-    const size_t ab = ((size_t)p.N * 8 + 15) & ~(size_t)15;
     s.x = reinterpret_cast<Pop*>(base);
     s.xn = reinterpret_cast<Pop*>(base + xb);
-    s.a = reinterpret_cast<float*>(base + xb + ab);
+    s.a = reinterpret_cast<float*>(base + 2 * xb);
     return s;
 }
 
@@ -281,10 +280,10 @@ __global__ void __launch_bounds__(256) k_batch(BatchParams bp) {
 // ---------------------------------------------------------------------------
 // Plain form: one thread per realization, one launch per step, FP32 time.
 // ---------------------------------------------------------------------------
-// Bytes of one plain-form realization's x and aux regions in HBM.
+// Bytes of one plain-form realization's two state buffers in HBM.
 template <class Pop>
 TL_HD size_t plain_slot_bytes(const SimParams& p) {
-    return (((size_t)p.N * sizeof(Pop) + 15) & ~(size_t)15) + (((size_t)p.N * 8 + 15) & ~(size_t)15);
+    return 2 * (((size_t)p.N * sizeof(Pop) + 15) & ~(size_t)15);
 }
 
 struct PlainState {
@@ -322,8 +321,13 @@ __global__ void k_plain_step(SimParams p, float* a_all) {
     PlainState* ps = reinterpret_cast<PlainState*>(p.pstate) + w;
     PlainState q = *ps;
     if (q.done) return;
-    // state and update scratch in HBM: x | aux (one thread scatters, in place)
+    // both state buffers in HBM; q.par says which holds the current state
     Slot<Pop> s = carve_slot<Pop>(reinterpret_cast<unsigned char*>(p.pslots) + (size_t)w * plain_slot_bytes<Pop>(p), p);
+    if (q.par) {
+        Pop* t = s.x;
+        s.x = s.xn;
+        s.xn = t;
+    }
     s.a = a_all + (size_t)w * p.M;
     Pop* const x_before = s.x;
     const int set = (int)(w / p.R);
