@@ -302,14 +302,39 @@ def run_ours(args, wl, rank, world, local_rank):
     }
     # end to end through the C ABI with host buffers
     if rank == 0:
-        line["e2e"] = e2e(args, wl, m, R, stream, sptr)
+        line["e2e"] = e2e(args, wl, m, R, T, stream, sptr)
         line["clocks"] = clk.summary()
+        if world == 1 and not args.no_plain:
+            line["plain_form"] = plain_form(args, wl, m, R, T, tot_ms / args.steps, sptr)
         if world == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline(args, wl, m, R)
         print(json.dumps(line), flush=True)
 
 
-def e2e(args, wl, m, R, stream, sptr):
+def plain_form(args, wl, m, R, T, fused_ms, sptr, budget_s: float = 8.0):
+    """The plain form (FP32 time, one realization per thread, one launch per
+    leap) beside the fused kernel, both on the same sample: all R
+    realizations to a t_final shortened, where needed, so that the plain run
+    takes about budget_s (its cost is estimated at 40x the fused run's)."""
+    from tau_leaping_gb300 import _ffi
+    frac = min(1.0, budget_s * 1e3 / max(40.0 * fused_ms, 1e-3))
+    Ts = T * frac
+    kw = dict(t_final=Ts, n=R, seed=args.seed, tracked=wl["tracked"], stream=sptr,
+              realization_offset=0)
+    out = {}
+    for name, var in (("plain", _ffi.VARIANT_PLAIN), ("fused", args.variant)):
+        m.simulate(**{**kw, "t_final": Ts * 0.1}, variant=var)
+        r = m.simulate(**kw, variant=var)
+        out[name] = dict(value=(r.leaps + r.ssa_steps) / (r.total_ms / 1e3), ms=r.total_ms,
+                         launches=r.launches, leaps=r.leaps, ssa_steps=r.ssa_steps)
+    return {"value": out["plain"]["value"], "unit": UNIT, "fused_value": out["fused"]["value"],
+            "speedup": out["fused"]["value"] / out["plain"]["value"],
+            "plain_ms": out["plain"]["ms"], "fused_ms": out["fused"]["ms"],
+            "plain_launches": out["plain"]["launches"], "sample": f"{R} realizations to t_final {Ts:.4g}",
+            "note": "host wall time of each tl_simulate call (kernels + statistics), same sample"}
+
+
+def e2e(args, wl, m, R, T, stream, sptr):
     """Same metric through tl_model_create + tl_simulate from host arrays:
     every step uploads the model, runs, and reads the statistics back."""
     import torch
@@ -325,7 +350,7 @@ def e2e(args, wl, m, R, stream, sptr):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         mm = Model.from_arrays(d["x0"], d["rate"], d["col_ptr"], d["row_ind"], d["stoich"], pop_bits=m.pop_bits)
-        r = mm.simulate(wl["t_final"], R, seed=args.seed, tracked=tr, variant=args.variant, stream=sptr)
+        r = mm.simulate(T, R, seed=args.seed, tracked=tr, variant=args.variant, stream=sptr)
         mm.close()
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
@@ -393,6 +418,7 @@ def main():
     ap.add_argument("--variant", type=int, default=0)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
     ap.add_argument("--batch-scale", type=float, default=1.0)
     ap.add_argument("--t-final", type=float, default=0.0, help="override t_final (profiling captures)")
     args = ap.parse_args()

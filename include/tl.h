@@ -163,6 +163,9 @@ enum tl_variant {
 #define TL_FLAG_NO_STAGE (1u << 3)       /* read model tables through L1/L2
                                             instead of staging them in
                                             shared memory (tuning knob)     */
+#define TL_FLAG_GRAPH (1u << 4)          /* PLAIN: replay the per-step launches
+                                            as a captured CUDA graph of 16
+                                            steps between completion polls  */
 /* Reference-compatibility switches (each reproduces one behaviour of the
  * shipped reference; default off = Cao-Gillespie-Petzold 2006 semantics). */
 #define TL_FLAG_COMPAT_G (1u << 8)       /* g read from channel order at the

@@ -673,18 +673,44 @@ static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad
         } else {
             le = w == 8 ? launch_plain_init<long long>(p, st) : launch_plain_init<int>(p, st);
             launches = 1;
+            // With TL_FLAG_GRAPH the 16 step launches between two polls are
+            // captured once (on a private stream) and replayed as one graph.
+            cudaGraphExec_t gexec = nullptr;
+            if (le == cudaSuccess && (cfg->flags & TL_FLAG_GRAPH)) {
+                cudaStream_t cs = nullptr;
+                le = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+                if (le == cudaSuccess) {
+                    cudaGraph_t g = nullptr;
+                    le = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+                    for (int q = 0; q < 16 && le == cudaSuccess; ++q)
+                        le = w == 8 ? launch_plain_step<long long>(p, J.rb.a_all, cs)
+                                    : launch_plain_step<int>(p, J.rb.a_all, cs);
+                    const cudaError_t ec = cudaStreamEndCapture(cs, &g);
+                    if (le == cudaSuccess) le = ec;
+                    if (le == cudaSuccess) le = cudaGraphInstantiate(&gexec, g, 0);
+                    if (g) cudaGraphDestroy(g);
+                    cudaStreamDestroy(cs);
+                }
+            }
             unsigned long long* hdone = nullptr;
             cudaMallocHost(&hdone, 8);
             while (le == cudaSuccess) {
-                for (int q = 0; q < 16 && le == cudaSuccess; ++q) {
-                    le = w == 8 ? launch_plain_step<long long>(p, J.rb.a_all, st) : launch_plain_step<int>(p, J.rb.a_all, st);
-                    ++launches;
+                if (gexec) {
+                    le = cudaGraphLaunch(gexec, st);
+                    launches += 16;
+                } else {
+                    for (int q = 0; q < 16 && le == cudaSuccess; ++q) {
+                        le = w == 8 ? launch_plain_step<long long>(p, J.rb.a_all, st)
+                                    : launch_plain_step<int>(p, J.rb.a_all, st);
+                        ++launches;
+                    }
                 }
                 if (le != cudaSuccess) break;
                 le = cudaMemcpyAsync(hdone, J.rb.ctr + 6, 8, cudaMemcpyDeviceToHost, st);
                 if (le == cudaSuccess) le = cudaStreamSynchronize(st);
                 if (le == cudaSuccess && *hdone >= (unsigned long long)J.total) break;
                 if (launches > (1 << 26)) {  // a realization that never ends
+                    if (gexec) cudaGraphExecDestroy(gexec);
                     cudaFreeHost(hdone);
                     cudaEventDestroy(e0);
                     cudaEventDestroy(e1);
@@ -692,6 +718,7 @@ static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad
                     return TL_ERR_STEP_CAP;
                 }
             }
+            if (gexec) cudaGraphExecDestroy(gexec);
             cudaFreeHost(hdone);
             if (le == cudaSuccess) le = launch_plain_tally(p, st);
             ++launches;

@@ -285,6 +285,13 @@ static __device__ __noinline__ int poisson_rare(float mu, float q, uint32_t j, u
 // Propensity and criticality of one channel (functions.h:100-123).
 // chan = {s0, s1, order, reference order}; order 0 = no reactant (a = c).
 // ---------------------------------------------------------------------------
+// Population to FP32.  int64 -> float runs at the reduced FP64 rate; an
+// int64 population that fits in int32 (the usual case) takes the 32-bit
+// conversion, which rounds to the same float.
+TL_D float popf(int x) { return (float)x; }
+static __device__ __noinline__ float popf_wide(long long x) { return (float)x; }
+TL_D float popf(long long x) { return (long long)(int)x == x ? (float)(int)x : popf_wide(x); }
+
 template <class Pop>
 TL_D void propensity(const int4 ch, float c, const Pop* x, int nc, bool compat_crit, float& a,
                      bool& crit) {
@@ -295,8 +302,10 @@ TL_D void propensity(const int4 ch, float c, const Pop* x, int nc, bool compat_c
     // halving exact.
     const int order = ch.z;
     const Pop x0 = x[ch.x], x1 = x[ch.y];
-    const float f0 = order == 0 ? 1.f : (float)x0;
-    const float f1 = order == 2 ? (float)x1 : order == 3 ? (float)(x0 - 1) * 0.5f : 1.f;
+    // second factor picked as an integer first: two conversions per channel
+    const Pop y = order == 2 ? x1 : order == 3 ? x0 - 1 : (Pop)1;
+    const float f0 = order == 0 ? 1.f : popf(x0);
+    const float f1 = popf(y) * (order == 3 ? 0.5f : 1.f);
     a = c * f0 * f1;
     const Pop t0 = order == 3 ? (compat_crit ? (Pop)((nc + 1) / 2) : (Pop)(2 * nc)) : (Pop)nc;
     crit = order != 0 && (x0 < t0 || (order == 2 && x1 < (Pop)nc));
@@ -384,7 +393,8 @@ struct GWarp {
 };
 
 // Whole CTA; needs a shared scratch of 34 doubles.  Every member is a
-// CTA-wide collective (call from all threads, uniform control flow).
+// CTA-wide collective (call from all threads, uniform control flow).  The
+// scratch holds each value in its own type (FP32 reductions stay FP32).
 struct GCta {
     static constexpr int kWidth = 0;
     int tid, n, lane, warp, nwarps;
@@ -396,35 +406,37 @@ struct GCta {
     TL_D float sumf(float v) const { return reduce_sum<float>(v); }
     template <class T>
     TL_D T reduce_sum(T v) const {
+        T* rt = reinterpret_cast<T*>(red);
 #pragma unroll
         for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         __syncthreads();
-        if (lane == 0) red[warp] = (double)v;
+        if (lane == 0) rt[warp] = v;
         __syncthreads();
         if (warp == 0) {
-            T x = lane < nwarps ? (T)red[lane] : (T)0;
+            T x = lane < nwarps ? rt[lane] : (T)0;
 #pragma unroll
             for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-            if (lane == 0) red[33] = (double)x;
+            if (lane == 0) *reinterpret_cast<T*>(red + 33) = x;
         }
         __syncthreads();
-        return (T)red[33];
+        return *reinterpret_cast<const T*>(red + 33);
     }
     TL_D double sumd(double v) const { return reduce_sum<double>(v); }
     TL_D float minf(float v) const {
+        float* rf = reinterpret_cast<float*>(red);
 #pragma unroll
         for (int o = 16; o; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
         __syncthreads();
-        if (lane == 0) red[warp] = (double)v;
+        if (lane == 0) rf[warp] = v;
         __syncthreads();
         if (warp == 0) {
-            float x = lane < nwarps ? (float)red[lane] : kInfF;
+            float x = lane < nwarps ? rf[lane] : kInfF;
 #pragma unroll
             for (int o = 16; o; o >>= 1) x = fminf(x, __shfl_xor_sync(0xffffffffu, x, o));
-            if (lane == 0) red[33] = (double)x;
+            if (lane == 0) rf[66] = x;
         }
         __syncthreads();
-        return (float)red[33];
+        return rf[66];
     }
     TL_D bool any(bool p) const { return __syncthreads_or(p ? 1 : 0) != 0; }
     TL_D double excl_scan(double v) const {
@@ -484,10 +496,11 @@ struct GCta {
     }
     template <class T>
     TL_D T bcast(T v, int src) const {
+        static_assert(sizeof(T) <= 8, "bcast of a value wider than 8 bytes");
         __syncthreads();
-        if (tid == src) red[32] = (double)v;
+        if (tid == src) *reinterpret_cast<T*>(red + 32) = v;
         __syncthreads();
-        const T r = (T)red[32];
+        const T r = *reinterpret_cast<const T*>(red + 32);
         __syncthreads();
         return r;
     }
@@ -620,7 +633,7 @@ template <class Pop>
 TL_D float species_bound(const SimParams& p, const MView& mv, const Pop* x, const float* a, int i,
                          float mu, float s2) {
     const bool cg = flag(p.flags, TL_FLAG_COMPAT_G);
-    const float xi = (float)x[i];
+    const float xi = popf(x[i]);
     float gi;
     if (cg) {
         const int ord = i < p.M ? mv.chan[i].w : 0;
@@ -679,6 +692,7 @@ TL_D float pass_tau(const Grp& g, const SimParams& p, const MView& mv, const Pop
             if (!all_rows && mv.gkind[i] == 0 && !OUT) continue;
             float mu = 0.f, s2 = 0.f;
             const int e = mv.rp[i + 1];
+#pragma unroll 4
             for (int q = mv.rp[i]; q < e; ++q) {
                 const int pk = mv.vc[q];
                 // critical channels are stored negative: max(a, 0) drops them
@@ -732,6 +746,7 @@ TL_D bool pass_update(const Grp& g, const SimParams& p, const MView& mv, const P
             const int i = mv.perm[ii];
             long long d = 0;
             const int e = mv.urp[i + 1];
+#pragma unroll 4
             for (int q = mv.urp[i]; q < e; ++q) {
                 const int pk = mv.uvc[q];
                 d += (long long)unpack_v(pk) * (long long)k[unpack_idx(pk)];
@@ -831,9 +846,13 @@ TL_D void pass_fire(const Grp& g, const SimParams& p, float* a, float tauf, int 
 #pragma unroll
             for (int e = 0; e < 4; ++e) av[e] = j0 + e < p.M ? a[j0 + e] : -0.f;
         }
+        // the shared block feeds only the k = 0 tests of means in (0, 10)
         bool need = false;
 #pragma unroll
-        for (int e = 0; e < 4; ++e) need |= !is_crit(av[e]) && av[e] * tauf > 0.f;
+        for (int e = 0; e < 4; ++e) {
+            const float m = av[e] * tauf;
+            need |= !is_crit(av[e]) && m > 0.f && m < 10.f;
+        }
         U4 gw{0u, 0u, 0u, 0u};
         if (need && !refs) gw = group_words(p.k0, p.k1, (uint32_t)g4, step, r, set);
         int kv[4];
@@ -969,7 +988,8 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
 
     // ---- tau-leap with negative-population rejection (CGP 2006 steps 3-5) ----
     const TimeT t_next = grid_time<TimeT>(p, T, st.kpt);
-    TimeT tau;
+    TimeT t_new;      // time after the leap (unless clamped to t_next)
+    float tau_used;   // the leap's tau
     bool clamp;
     for (int attempt = 0;; ++attempt) {
         const float a0cf = g.sumf(pac);
@@ -986,20 +1006,20 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
                 tau2 = -logf(u01f(w.x)) / a0cf;
             }
         }
-        tau = (TimeT)fminf(tau1, tau2);
+        float tauf = fminf(tau1, tau2);
         bool fire = tau2 < tau1;
-        clamp = false;
-        if (st.t + tau >= t_next) {
-            tau = t_next - st.t;
-            clamp = true;
+        t_new = st.t + (TimeT)tauf;
+        clamp = t_new >= t_next;
+        if (clamp) {
+            tauf = (float)(t_next - st.t);
             fire = false;
         }
+        tau_used = tauf;
         if (fire && jc < 0) {
             const TimeT a0c = (TimeT)g.sumd((double)pac);
             jc = select_channel<Grp, TimeT>(g, p, s.a, pac, (TimeT)u01d(w.z, w.w) * a0c, 1);
         }
         if (!fire) jc = -1;
-        const float tauf = (float)tau;
         pass_fire<Grp>(g, p, s.a, tauf, jc, st.step, r, (uint32_t)set);
         int* kk = reinterpret_cast<int*>(s.a);
         g.sync();
@@ -1029,7 +1049,7 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
     if (SENS && score) {
         // score_j += (k_j - a_j*tau)/c_j with a_j recomputed from the old state
         const bool cc = flag(f, TL_FLAG_COMPAT_CRIT);
-        const float tauf = (float)tau;
+        const float tauf = tau_used;
         const int* kk = reinterpret_cast<const int*>(s.a);
         for (int m = g.rank(); m < p.M; m += g.size()) {
             const float c = __ldg(rate + m);
@@ -1047,7 +1067,7 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
         s.x = s.xn;
         s.xn = t;
     }
-    st.t = clamp ? t_next : st.t + tau;
+    st.t = clamp ? t_next : t_new;
     st.step++;
     st.leaps++;
     st.nsteps++;

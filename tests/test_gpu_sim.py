@@ -77,6 +77,18 @@ def test_deterministic_and_variant_independent_streams():
     assert np.array_equal(a.samples, c.samples), "scheduling must not change a realization"
 
 
+def test_plain_graph_replay_is_bit_identical():
+    """The graph-captured plain step loop launches the same kernels."""
+    m = Model.generate("toy")
+    kw = dict(t_final=0.01, n=700, seed=4, tracked=[0, 4], keep_samples=True, intervals=3,
+              variant=_ffi.VARIANT_PLAIN)
+    a = m.simulate(**kw)
+    b = m.simulate(flags=_ffi.FLAG_GRAPH, **kw)
+    assert np.array_equal(a.samples, b.samples)
+    assert (a.leaps, a.ssa_steps, a.rejections) == (b.leaps, b.ssa_steps, b.rejections)
+    assert a.launches == b.launches
+
+
 def test_rate_sets_are_independent_of_batch_neighbours():
     m = dimer()
     base = m.desc()["rate"]
