@@ -24,6 +24,7 @@ STATUS = {
 }
 
 VARIANT_AUTO, VARIANT_THREAD, VARIANT_WARP, VARIANT_CTA, VARIANT_PLAIN = 0, 1, 2, 3, 4
+VARIANT_LANES2, VARIANT_LANES4, VARIANT_LANES8, VARIANT_LANES16 = 5, 6, 7, 8
 FLAG_SENSITIVITY = 1 << 0
 FLAG_KEEP_SAMPLES = 1 << 1
 FLAG_AUTOTUNE_MEASURE = 1 << 2

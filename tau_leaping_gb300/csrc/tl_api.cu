@@ -221,6 +221,10 @@ static tl_status make_plan(const tl_model* m, int variant, int block_req, bool s
         pl.kind = 32;
         pl.block = block_req > 0 ? block_req : 256;
         groups_per_block = pl.block / 32;
+    } else if (variant >= TL_VARIANT_LANES2 && variant <= TL_VARIANT_LANES16) {
+        pl.kind = 2 << (variant - TL_VARIANT_LANES2);
+        pl.block = block_req > 0 ? block_req : 256;
+        groups_per_block = pl.block / pl.kind;
     } else if (variant == TL_VARIANT_CTA) {
         pl.kind = 0;
         pl.block = block_req > 0 ? block_req : (sb <= 64 * 1024 ? 256 : 1024);
@@ -237,7 +241,7 @@ static tl_status make_plan(const tl_model* m, int variant, int block_req, bool s
     // shrink the block until the slots fit
     while ((size_t)groups_per_block * sb > (size_t)smax && pl.kind != 0 && pl.block > 32) {
         pl.block -= 32;
-        groups_per_block = pl.kind == 1 ? pl.block : pl.block / 32;
+        groups_per_block = pl.block / pl.kind;
     }
     if ((size_t)groups_per_block * sb > (size_t)smax) {
         set_last_error("model too large for the shared-memory slot of this variant");
@@ -568,6 +572,9 @@ static tl_status autotune_measure(Job& J, cudaStream_t st) {
         std::vector<Cand> cands;
         if (m->h.M <= 64 && m->h.N <= 64)
             for (int b : {32, 64, 128}) cands.push_back({TL_VARIANT_THREAD, b, false});
+        if (m->h.M <= 1024)
+            for (int v = TL_VARIANT_LANES2; v <= TL_VARIANT_LANES16; ++v)
+                for (int b : {128, 256}) cands.push_back({v, b, false});
         for (int b : {64, 128, 256})
             for (bool ns : {false, true}) cands.push_back({TL_VARIANT_WARP, b, ns});
         for (int b : {64, 128, 256, 512, 1024})

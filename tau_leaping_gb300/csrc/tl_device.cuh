@@ -207,17 +207,40 @@ TL_HD U4 group_words(uint32_t k0, uint32_t k1, uint32_t g, uint32_t step, uint32
     return philox10(U4{g, step, r, (set << 8) | 0xFFu}, k0, k1);
 }
 
-// Poisson(mu) from one 32-bit word w for mu < 10: q = (w + 1/2) 2^-32 is
-// uniform on (0,1) with full relative precision near 0, so the k = 0 test
-// q >= P(K >= 1) = -expm1(-mu) stays exact for tiny means (a 23-bit
-// uniform would quantise it); k >= 1 continues the sequential inversion on
+// P(K >= 1) = 1 - exp(-mu) for 0 < mu: below 0.1 the Taylor series to
+// mu^6 (truncation < mu^7/5040, relative 2e-10), above it 1 - expf(-mu)
+// (relative error < 1.2e-6: expf is within 2 ulp and exp(-mu) < 0.905).
+TL_D float poisson_p1(float mu) {
+    if (mu < 0.1f)
+        return mu * (1.f - mu * (0.5f - mu * (1.f / 6.f - mu * (1.f / 24.f - mu * (1.f / 120.f - mu * (1.f / 720.f))))));
+    return 1.f - expf(-mu);
+}
+
+// P(K >= 2) = 1 - exp(-mu)(1 + mu) for 0 < mu < 10: below 0.5 the series
+// sum_{n>=2} (-1)^n (n-1) mu^n / n! to n = 9 (relative error < 3e-8), above
+// it directly (exp(-mu)(1 + mu) < 0.91 there: relative error < 1.3e-6).
+TL_D float poisson_p2(float mu) {
+    if (mu < 0.5f) {
+        const float c = 0.5f + mu * (-1.f / 3.f + mu * (1.f / 8.f + mu * (-1.f / 30.f + mu * (1.f / 144.f +
+                        mu * (-1.f / 840.f + mu * (1.f / 5760.f - mu * (1.f / 45360.f)))))));
+        return mu * mu * c;
+    }
+    return 1.f - expf(-mu) * (1.f + mu);
+}
+
+// Poisson(mu) for mu < 10 from one 32-bit word w by inversion with
+// q = (w + 1/2) 2^-32, which is uniform on (0,1) with full relative precision
+// near 0: k = 0 iff q >= P(K >= 1), k = 1 iff P(K >= 2) <= q < P(K >= 1).
+// Both tests are exact for the tiny means that dominate (a 23-bit uniform
+// would quantise them); k >= 2 continues the sequential inversion on
 // u = 1 - q.  mu >= 10 uses PTRS on the private stream.
 template <class Rng>
-TL_D int poisson_first_tail(float mu, float q, Rng& rng) {
+TL_D int poisson_tail2(float mu, float q, Rng& rng) {
     if (mu >= 10.f) return poisson_ptrs(mu, rng);
     const float u = 1.f - q;
-    float p = expf(-mu), F = p;
-    for (int k = 1; k < 64; ++k) {
+    const float e = expf(-mu);
+    float p = e * mu, F = e + p;
+    for (int k = 2; k < 64; ++k) {
         p = p * __fdividef(mu, (float)k);
         const float Fn = F + p;
         if (u <= Fn) return k;
@@ -232,10 +255,10 @@ TL_D int poisson_first(float mu, uint32_t w, Rng& rng) {
     if (!(mu > 0.f)) return 0;
     if (mu >= 10.f) return poisson_ptrs(mu, rng);
     const float q = ((float)w + 0.5f) * 2.3283064365386963e-10f;
-    // P(K >= 1) = 1 - exp(-mu); Taylor series below 0.01 (error < mu^4/24)
-    const float s0 = mu < 0.01f ? mu * (1.f - mu * (0.5f - mu * (1.f / 6.f))) : -expm1f(-mu);
+    const float s0 = poisson_p1(mu);
     if (q >= s0) return 0;
-    return poisson_first_tail(mu, q, rng);
+    if (q >= poisson_p2(mu)) return 1;
+    return poisson_tail2(mu, q, rng);
 }
 
 TL_D uint32_t word_of(const U4& w, int e) { return e == 0 ? w.x : e == 1 ? w.y : e == 2 ? w.z : w.w; }
@@ -265,7 +288,7 @@ TL_D int poisson_reference(float mu, Rng& rng) {
     return (int)fabsf(mu + sqrtf(mu) * z);
 }
 
-// The draw of one channel once its k = 0 test has failed (or its mean is
+// The draw of one channel once its k <= 1 tests have failed (or its mean is
 // >= 10, or the reference's sampler is asked for), out of line: it is the
 // rare path of a leap, and keeping it out of the unrolled channel loop keeps
 // the hot loop small in the instruction cache.
@@ -274,7 +297,7 @@ TL_D int poisson_rare_inline(float mu, float q, uint32_t j, uint32_t step, uint3
     ChanRng rng;
     rng.init(j, step, r, set, k0, k1);
     if (refs) return poisson_reference(mu, rng);
-    return poisson_first_tail(mu, q, rng);
+    return poisson_tail2(mu, q, rng);
 }
 static __device__ __noinline__ int poisson_rare(float mu, float q, uint32_t j, uint32_t step, uint32_t r,
                                                 uint32_t set, uint32_t k0, uint32_t k1, int refs) {
@@ -389,6 +412,68 @@ struct GWarp {
     template <class T>
     TL_D T bcast(T v, int src) const {
         return __shfl_sync(0xffffffffu, v, src);
+    }
+};
+
+// W lanes of one warp (W = 2, 4, 8, 16): lanes [base, base + W).  Shuffles
+// run on W-lane segments with the group's own mask, so the groups of a warp
+// advance independently (different realizations take different paths).
+template <int W>
+struct GSub {
+    static_assert(W >= 2 && W <= 16 && (W & (W - 1)) == 0, "sub-warp width");
+    static constexpr int kWidth = W;
+    int lane;       // rank in the group
+    int base;       // first lane of the group in its warp
+    unsigned mask;  // the group's lanes
+    static TL_D GSub make() {
+        GSub g;
+        const int l = (int)(threadIdx.x & 31);
+        g.lane = l & (W - 1);
+        g.base = l & ~(W - 1);
+        g.mask = (W == 32 ? 0xffffffffu : ((1u << W) - 1u)) << g.base;
+        return g;
+    }
+    TL_D int rank() const { return lane; }
+    TL_D int size() const { return W; }
+    TL_D void sync() const { __syncwarp(mask); }
+    TL_D bool leader() const { return lane == 0; }
+    TL_D float sumf(float v) const {
+#pragma unroll
+        for (int o = W / 2; o; o >>= 1) v += __shfl_xor_sync(mask, v, o, W);
+        return v;
+    }
+    TL_D double sumd(double v) const {
+#pragma unroll
+        for (int o = W / 2; o; o >>= 1) v += __shfl_xor_sync(mask, v, o, W);
+        return v;
+    }
+    TL_D float minf(float v) const {
+#pragma unroll
+        for (int o = W / 2; o; o >>= 1) v = fminf(v, __shfl_xor_sync(mask, v, o, W));
+        return v;
+    }
+    TL_D bool any(bool p) const { return (__ballot_sync(mask, p) & mask) != 0u; }
+    TL_D double excl_scan(double v) const {
+        double s = v;
+#pragma unroll
+        for (int o = 1; o < W; o <<= 1) {
+            const double n = __shfl_up_sync(mask, s, o, W);
+            if (lane >= o) s += n;
+        }
+        const double e = __shfl_up_sync(mask, s, 1, W);
+        return lane ? e : 0.0;
+    }
+    TL_D int first(bool p) const {
+        const unsigned b = (__ballot_sync(mask, p) & mask) >> base;
+        return b ? __ffs(b) - 1 : -1;
+    }
+    TL_D int last(bool p) const {
+        const unsigned b = (__ballot_sync(mask, p) & mask) >> base;
+        return b ? 31 - __clz(b) : -1;
+    }
+    template <class T>
+    TL_D T bcast(T v, int src) const {
+        return __shfl_sync(mask, v, src, W);
     }
 };
 
@@ -786,6 +871,11 @@ __device__ __noinline__ int select_channel_impl(const Grp g, const int M, const 
     if (g.rank() == L) {
         float acc = 0.f;
         int lastpos = -1;
+        // Inside the lane the search runs on the lane's FP32 running sum:
+        // the offset into the lane, target - excl (FP64), rounded toward
+        // -inf, so that for a float acc  rd(t) < acc  <=>  t < acc exactly.
+        const AccT trem = target - excl;
+        const float tf = sizeof(AccT) == 8 ? __double2float_rd((double)trem) : (float)trem;
         for (int j = g.rank(); j < M; j += g.size()) {
             const float aj = a[j];
             const bool c = is_crit(aj);
@@ -794,7 +884,7 @@ __device__ __noinline__ int select_channel_impl(const Grp g, const int M, const 
             if (!(v > 0.f)) continue;
             acc += v;
             lastpos = j;
-            if (target < excl + (AccT)acc) {
+            if (tf < acc) {
                 sel = j;
                 break;
             }
@@ -867,10 +957,18 @@ TL_D void pass_fire(const Grp& g, const SimParams& p, float* a, float tauf, int 
                 float q = 0.f;
                 bool rare = refs && mu > 0.f;
                 if (!refs && mu > 0.f) {
-                    // hot path: the k = 0 test of poisson_first on the shared word
+                    // hot path: the k = 0 and k = 1 tests of poisson_first on
+                    // the shared word
                     q = ((float)word_of(gw, e) + 0.5f) * 2.3283064365386963e-10f;
-                    const float s0 = mu < 0.01f ? mu * (1.f - mu * (0.5f - mu * (1.f / 6.f))) : -expm1f(-mu);
-                    rare = mu >= 10.f || q < s0;
+                    if (mu >= 10.f) {
+                        rare = true;
+                    } else {
+                        const float s0 = poisson_p1(mu);
+                        if (q < s0) {
+                            if (q >= poisson_p2(mu)) k = 1;
+                            else rare = true;
+                        }
+                    }
                 }
                 if (rare) {
                     // thread groups inline the rare draw (their loop is per
@@ -940,12 +1038,9 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
             const U4 w = step_words(p.k0, p.k1, st.step, r, (uint32_t)set);
             const TimeT target = (TimeT)u01d(w.z, w.w) * a0;
             const int j = select_channel<Grp, TimeT>(g, p, s.a, pa, target, 0);
-            TimeT dt;
-            if (flag(f, TL_FLAG_COMPAT_TAU2)) {
-                dt = (TimeT)(-logf(u01f(w.x))) / (TimeT)fabsf(s.a[j]);
-            } else {
-                dt = (TimeT)(-logf(u01f(w.x))) / a0;
-            }
+            // the waiting time in FP32 (FP64 keeps only the time sum)
+            const float ex = -logf(u01f(w.x));
+            const TimeT dt = (TimeT)(flag(f, TL_FLAG_COMPAT_TAU2) ? ex / fabsf(s.a[j]) : ex / (float)a0);
             while (st.kpt <= p.n_int && st.t + dt >= grid_time<TimeT>(p, T, st.kpt))
                 record_point<Grp, Pop>(g, p, s.x, samp, st.kpt++);
             if (st.kpt > p.n_int) {

@@ -105,8 +105,13 @@ TL_D Slot<Pop> carve_slot(unsigned char* base, const SimParams& p) {
     return s;
 }
 
+// KIND: 1 = thread, 32 = warp, 0 = CTA, 2/4/8/16 = that many lanes of a warp.
 template <int KIND>
-struct GroupOf;
+struct GroupOf {
+    using type = GSub<KIND>;
+    static TL_D GSub<KIND> make(double*) { return GSub<KIND>::make(); }
+    static TL_D int index() { return threadIdx.x / KIND; }
+};
 template <>
 struct GroupOf<1> {
     using type = G1;

@@ -4,7 +4,7 @@
 //
 //   tl_cli -f model.xml -t T -n R -r S1 S5 [-e eps] [-i intervals]
 //          [-a max_steps] [-b name] [-d device]
-//          [--seed S] [--compat] [--variant auto|thread|warp|cta|plain]
+//          [--seed S] [--compat] [--variant auto|thread|lanes2|lanes4|lanes8|lanes16|warp|cta|plain]
 //          [--pop64] [--samples file]
 //
 // Writes mean_<name>.txt and stddev_<name>.txt, one line per grid time
@@ -50,7 +50,7 @@ struct Args {
 void usage() {
     std::cerr << "usage: tl_cli -f <model.xml> -t <t_final> -n <realizations> -r <species ...|all>\n"
                  "              [-e eps] [-i intervals] [-a max_steps] [-b name] [-d device]\n"
-                 "              [--seed S] [--compat] [--variant auto|thread|warp|cta|plain] [--pop64]\n"
+                 "              [--seed S] [--compat] [--variant auto|thread|lanes2|lanes4|lanes8|lanes16|warp|cta|plain] [--pop64]\n"
                  "              [--samples file]\n";
 }
 
@@ -113,7 +113,9 @@ bool parse(int argc, char** argv, Args& a) {
             if (!(v = need("--variant"))) return false;
             const std::string s = v;
             a.variant = s == "thread" ? TL_VARIANT_THREAD : s == "warp" ? TL_VARIANT_WARP
-                      : s == "cta" ? TL_VARIANT_CTA : s == "plain" ? TL_VARIANT_PLAIN : TL_VARIANT_AUTO;
+                      : s == "cta" ? TL_VARIANT_CTA : s == "plain" ? TL_VARIANT_PLAIN
+                      : s == "lanes2" ? TL_VARIANT_LANES2 : s == "lanes4" ? TL_VARIANT_LANES4
+                      : s == "lanes8" ? TL_VARIANT_LANES8 : s == "lanes16" ? TL_VARIANT_LANES16 : TL_VARIANT_AUTO;
         } else if (k == "-h" || k == "--help") {
             usage();
             exit(0);

@@ -30,7 +30,9 @@ def compare_final(a, b, label, p=P99):
         assert pt > p and pl > p and pk > p, f"{label} species {k}: t {pt:.3g} levene {pl:.3g} ks {pk:.3g}"
 
 
-@pytest.mark.parametrize("variant", [_ffi.VARIANT_THREAD, _ffi.VARIANT_WARP, _ffi.VARIANT_CTA, _ffi.VARIANT_PLAIN])
+@pytest.mark.parametrize("variant", [_ffi.VARIANT_THREAD, _ffi.VARIANT_WARP, _ffi.VARIANT_CTA, _ffi.VARIANT_PLAIN,
+                                     _ffi.VARIANT_LANES2, _ffi.VARIANT_LANES4, _ffi.VARIANT_LANES8,
+                                     _ffi.VARIANT_LANES16])
 def test_dimer_tau_leap_matches_oracle(variant):
     m = dimer()
     o = ora.OracleModel.from_desc(m.desc())
@@ -75,6 +77,9 @@ def test_deterministic_and_variant_independent_streams():
     assert (a.leaps, a.ssa_steps, a.rejections) == (b.leaps, b.ssa_steps, b.rejections)
     c = m.simulate(variant=_ffi.VARIANT_WARP, block_threads=64, **kw)
     assert np.array_equal(a.samples, c.samples), "scheduling must not change a realization"
+    d = m.simulate(variant=_ffi.VARIANT_LANES4, block_threads=64, **kw)
+    e = m.simulate(variant=_ffi.VARIANT_LANES4, block_threads=256, **kw)
+    assert np.array_equal(d.samples, e.samples), "scheduling must not change a sub-warp realization"
 
 
 def test_plain_graph_replay_is_bit_identical():
@@ -167,6 +172,31 @@ def test_colloid_cta_matches_oracle():
     compare_final(w.samples[0, :, -1, :], r["samples"][0, :, -1, :], "colloid warp")
 
 
+def test_colloid_full_config_within_1pct_of_fp64_oracle(capsys):
+    """Colloidal aggregation, 250 species x 31250 channels, int64, t_final
+    0.01, 4096 realizations (the full configuration): the ensemble mean and
+    variance of every species agree with the FP64 oracle running the same
+    method within 1 % plus four combined standard errors; the errors are
+    reported."""
+    m = Model.generate("colloid")
+    N = m.n_species
+    g = m.simulate(0.01, 4096, seed=13, tracked=list(range(N)), keep_samples=True)
+    o = ora.OracleModel.from_desc(m.desc())
+    r = o.simulate(0.01, 4096, seed=14, tracked=list(range(N)), threads=8)
+    a, b = g.samples[0, :, -1, :].astype(float), r["samples"][0, :, -1, :].astype(float)
+    ma, mb, va, vb = a.mean(0), b.mean(0), a.var(0, ddof=1), b.var(0, ddof=1)
+    rel_m = np.abs(ma - mb) / mb
+    rel_v = np.abs(va - vb) / vb
+    se_m = np.sqrt(va / len(a) + vb / len(b)) / mb
+    se_v = np.sqrt(2.0 / (len(a) - 1) + 2.0 / (len(b) - 1))
+    with capsys.disabled():
+        print(f"\ncolloid-250 vs FP64 oracle (4096 + 4096 realizations): mean rel err max {rel_m.max():.2e} "
+              f"rms {np.sqrt((rel_m ** 2).mean()):.2e} (s.e. ~{np.median(se_m):.1e}); variance rel err max "
+              f"{rel_v.max():.2e} rms {np.sqrt((rel_v ** 2).mean()):.2e} (s.e. ~{se_v:.1e})")
+    assert np.all(rel_m <= 0.01 + 4 * se_m), rel_m.max()
+    assert np.all(rel_v <= 0.01 + 4 * se_v), rel_v.max()
+
+
 def test_measured_autotuner_picks_a_plan_and_caches_it():
     m = Model.generate("toy", n_species=32, n_channels=64, seed=4, x0_max=3000)
     o = ora.OracleModel.from_desc(m.desc())
@@ -181,7 +211,9 @@ def test_measured_autotuner_picks_a_plan_and_caches_it():
 
 
 @pytest.mark.parametrize("variant,block", [(_ffi.VARIANT_CTA, 64), (_ffi.VARIANT_CTA, 128), (_ffi.VARIANT_CTA, 256),
-                                           (_ffi.VARIANT_WARP, 64), (_ffi.VARIANT_THREAD, 32)])
+                                           (_ffi.VARIANT_WARP, 64), (_ffi.VARIANT_THREAD, 32),
+                                           (_ffi.VARIANT_LANES2, 64), (_ffi.VARIANT_LANES4, 128),
+                                           (_ffi.VARIANT_LANES8, 256), (_ffi.VARIANT_LANES16, 128)])
 def test_group_widths_agree_on_chain(variant, block):
     m = Model.generate("chain", n_species=48)
     o = ora.OracleModel.from_desc(m.desc())
