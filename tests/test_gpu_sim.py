@@ -203,7 +203,8 @@ def test_measured_autotuner_picks_a_plan_and_caches_it():
     flags = _ffi.FLAG_AUTOTUNE_MEASURE
     a = m.simulate(0.005, 3000, seed=3, tracked=[0, 1], flags=flags, keep_samples=True)
     b = m.simulate(0.005, 3000, seed=3, tracked=[0, 1], flags=flags, keep_samples=True)
-    assert a.variant in (_ffi.VARIANT_THREAD, _ffi.VARIANT_WARP, _ffi.VARIANT_CTA)
+    assert a.variant in (_ffi.VARIANT_THREAD, _ffi.VARIANT_WARP, _ffi.VARIANT_CTA, _ffi.VARIANT_LANES2,
+                         _ffi.VARIANT_LANES4, _ffi.VARIANT_LANES8, _ffi.VARIANT_LANES16)
     assert (a.variant, a.block_threads) == (b.variant, b.block_threads)
     assert np.array_equal(a.samples, b.samples)
     r = o.simulate(0.005, 1500, seed=4, tracked=[0, 1], threads=8)
