@@ -307,7 +307,7 @@ def run_ours(args, wl, rank, world, local_rank):
         if world == 1 and not args.no_plain:
             line["plain_form"] = plain_form(args, wl, m, R, T, tot_ms / args.steps, sptr)
         if world == 1 and not args.no_cpu:
-            line["cpu_baseline"] = cpu_baseline(args, wl, m, R)
+            line["cpu_baseline"] = cpu_baseline(args, wl, m, R, check_gpu=True)
         print(json.dumps(line), flush=True)
 
 
@@ -359,9 +359,10 @@ def e2e(args, wl, m, R, T, stream, sptr):
     return {"value": steps / tot, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
 
 
-def cpu_baseline(args, wl, m, R, budget_s: float = 12.0):
+def cpu_baseline(args, wl, m, R, budget_s: float = 12.0, check_gpu: bool = False):
     """FP64 oracle port of the reference's algorithm on the host cores, on a
-    bounded sample (the first realizations of the same ensemble)."""
+    bounded sample (the first realizations of the same ensemble).  With
+    check_gpu the same realizations also run on the GPU for fp64_check."""
     from oracle import py as ora
     o = ora.OracleModel.from_desc(m.desc())
     cores = os.cpu_count() or 1
@@ -370,6 +371,7 @@ def cpu_baseline(args, wl, m, R, budget_s: float = 12.0):
     r = o.simulate(wl["t_final"], R, seed=args.seed, tracked=wl["tracked"], threads=cores, r_begin=0, r_end=n)
     dt = time.perf_counter() - t0
     done, steps = n, r["leaps"] + r["ssa_steps"]
+    finals = [r["samples"][0, :, -1, :]]
     while dt < budget_s and done < R:
         k = min(R - done, max(cores, int(done * (budget_s - dt) / max(dt, 1e-3) * 0.8)))
         t1 = time.perf_counter()
@@ -378,8 +380,30 @@ def cpu_baseline(args, wl, m, R, budget_s: float = 12.0):
         dt += time.perf_counter() - t1
         done += k
         steps += r["leaps"] + r["ssa_steps"]
-    return {"value": steps / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{done} of {R} realizations of the same workload, FP64 oracle, {cores} threads, {dt:.1f} s"}
+        finals.append(r["samples"][0, :, -1, :])
+    out = {"value": steps / dt, "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": f"{done} of {R} realizations of the same workload, FP64 oracle, {cores} threads, {dt:.1f} s"}
+    if check_gpu:
+        out["fp64_check"] = fp64_check(args, wl, m, done, np.concatenate(finals).astype(np.float64))
+    return out
+
+
+def fp64_check(args, wl, m, n, ora_final):
+    """Error of the engine against the FP64 oracle on the baseline's sample:
+    the same n realizations (same ids, so the same Philox streams) run on
+    the GPU with their samples kept.  Reports, per tracked species, the
+    relative difference of the ensemble mean and variance at t_final and the
+    share of realizations whose final state is identical."""
+    g = m.simulate(wl["t_final"], n, seed=args.seed, tracked=wl["tracked"], keep_samples=True,
+                   variant=args.variant)
+    gf = g.samples[0, :, -1, :].astype(np.float64)
+    rel_mean = np.abs(gf.mean(0) - ora_final.mean(0)) / np.maximum(np.abs(ora_final.mean(0)), 1e-300)
+    var_o = ora_final.var(0, ddof=1) if n > 1 else np.zeros(gf.shape[1])
+    var_g = gf.var(0, ddof=1) if n > 1 else np.zeros(gf.shape[1])
+    rel_var = np.abs(var_g - var_o) / np.maximum(var_o, 1e-300)
+    return {"realizations": int(n), "tracked": wl["tracked"],
+            "mean_rel_err": [float(x) for x in rel_mean], "var_rel_err": [float(x) for x in rel_var],
+            "identical_final_state": float(np.mean(np.all(gf == ora_final, axis=1)))}
 
 
 def run_reference(args, wl, rank):
