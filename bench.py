@@ -401,8 +401,12 @@ def fp64_check(args, wl, m, n, ora_final):
     var_o = ora_final.var(0, ddof=1) if n > 1 else np.zeros(gf.shape[1])
     var_g = gf.var(0, ddof=1) if n > 1 else np.zeros(gf.shape[1])
     rel_var = np.abs(var_g - var_o) / np.maximum(var_o, 1e-300)
+    # one standard error of each difference, were the two samples independent
+    se_mean = np.sqrt((var_g + var_o) / max(n, 1)) / np.maximum(np.abs(ora_final.mean(0)), 1e-300)
+    se_var = np.sqrt(4.0 / max(n - 1, 1)) * np.ones_like(rel_var)
     return {"realizations": int(n), "tracked": wl["tracked"],
-            "mean_rel_err": [float(x) for x in rel_mean], "var_rel_err": [float(x) for x in rel_var],
+            "mean_rel_err": [float(x) for x in rel_mean], "mean_rel_se": [float(x) for x in se_mean],
+            "var_rel_err": [float(x) for x in rel_var], "var_rel_se": [float(x) for x in se_var],
             "identical_final_state": float(np.mean(np.all(gf == ora_final, axis=1)))}
 
 

@@ -197,7 +197,7 @@ static int heuristic_variant(const tl_model* m, size_t sb) {
     return TL_VARIANT_CTA;
 }
 
-static tl_status make_plan(const tl_model* m, int variant, int block_req, bool sens, bool compat_stoich,
+static tl_status make_plan(const tl_model* m, int variant, int block_req, bool gen, bool compat_stoich,
                            bool no_stage, long long total, Plan& pl) {
     const size_t sb = slot_bytes(m);
     const int smax = max_smem_optin() - 2048;
@@ -254,8 +254,8 @@ static tl_status make_plan(const tl_model* m, int variant, int block_req, bool s
     pl.smem = (size_t)pl.stage + (size_t)groups_per_block * sb;
     pl.row_warp = pl.kind == 0 && m->h.max_row > 32;
     int bps = 0;
-    cudaError_t e = m->h.pop_bits == 64 ? fused_occupancy<long long>(pl.kind, sens, pl.block, pl.smem, &bps)
-                                        : fused_occupancy<int>(pl.kind, sens, pl.block, pl.smem, &bps);
+    cudaError_t e = m->h.pop_bits == 64 ? fused_occupancy<long long>(pl.kind, gen, pl.block, pl.smem, &bps)
+                                        : fused_occupancy<int>(pl.kind, gen, pl.block, pl.smem, &bps);
     if (e != cudaSuccess) return cuda_fail(e, "occupancy");
     if (bps < 1) {
         set_last_error("the launch does not fit an SM");
@@ -293,6 +293,7 @@ struct Job {
     int S = 1, P = 2, K = 0;
     long long R = 1, total = 1;
     bool sens = false, keep = false, plain = false, compat_stoich = false;
+    bool gen = false;  // launch the general kernel (scores or compatibility switches)
     size_t w = 4;
     std::vector<float> hrates;
     std::vector<double> htf;
@@ -343,6 +344,7 @@ static tl_status job_prepare(Job& J) {
     J.K = cfg->n_tracked;
     J.total = J.R * J.S;
     J.sens = J.grad != nullptr;
+    J.gen = J.sens || (cfg->flags & TL_FLAG_COMPAT_REFERENCE) != 0;
     J.keep = (cfg->flags & TL_FLAG_KEEP_SAMPLES) != 0;
     J.plain = cfg->variant == TL_VARIANT_PLAIN;
     J.compat_stoich = (cfg->flags & TL_FLAG_COMPAT_STOICH) != 0;
@@ -591,14 +593,14 @@ static tl_status autotune_measure(Job& J, cudaStream_t st) {
         Cand win{0, 0, false};
         for (const Cand& c : cands) {
             Plan pl;
-            if (make_plan(m, c.variant, c.block, J.sens, J.compat_stoich, c.nostage, trial, pl) != TL_OK) continue;
+            if (make_plan(m, c.variant, c.block, J.gen, J.compat_stoich, c.nostage, trial, pl) != TL_OK) continue;
             if (c.variant == TL_VARIANT_THREAD && c.block != pl.block) continue;
             tp.stage_bytes = pl.stage;
             tp.row_warp = pl.row_warp ? 1 : 0;
             if (cudaMemsetAsync(tp.ctr, 0, 64, st) != cudaSuccess) break;
             cudaEventRecord(e0, st);
-            cudaError_t le = J.w == 8 ? launch_fused<long long>(tp, pl.kind, J.sens, pl.block, pl.grid, pl.smem, st)
-                                      : launch_fused<int>(tp, pl.kind, J.sens, pl.block, pl.grid, pl.smem, st);
+            cudaError_t le = J.w == 8 ? launch_fused<long long>(tp, pl.kind, J.gen, pl.block, pl.grid, pl.smem, st)
+                                      : launch_fused<int>(tp, pl.kind, J.gen, pl.block, pl.grid, pl.smem, st);
             cudaEventRecord(e1, st);
             if (le != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
                 cudaGetLastError();
@@ -623,7 +625,7 @@ static tl_status autotune_measure(Job& J, cudaStream_t st) {
         m->tuned_block = win.block;
         m->tuned_nostage = win.nostage ? 1 : 0;
     }
-    tl_status ps = make_plan(m, m->tuned_variant, m->tuned_block, J.sens, J.compat_stoich, m->tuned_nostage != 0,
+    tl_status ps = make_plan(m, m->tuned_variant, m->tuned_block, J.gen, J.compat_stoich, m->tuned_nostage != 0,
                              J.total, J.pl);
     if (ps != TL_OK) return ps;
     J.p.stage_bytes = J.pl.stage;
@@ -645,7 +647,7 @@ static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad
     const bool no_stage = (cfg->flags & TL_FLAG_NO_STAGE) != 0;
     const bool measure = !J.plain && cfg->variant == TL_VARIANT_AUTO && (cfg->flags & TL_FLAG_AUTOTUNE_MEASURE);
     if (!J.plain) {
-        ps = make_plan(m, cfg->variant, cfg->block_threads, J.sens, J.compat_stoich, no_stage, J.total, J.pl);
+        ps = make_plan(m, cfg->variant, cfg->block_threads, J.gen, J.compat_stoich, no_stage, J.total, J.pl);
         if (ps != TL_OK) return ps;
     } else {
         J.pl.variant = TL_VARIANT_PLAIN;
@@ -674,8 +676,8 @@ static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad
     cudaError_t le = cudaEventRecord(e0, st);
     if (le == cudaSuccess) {
         if (!J.plain) {
-            le = w == 8 ? launch_fused<long long>(p, J.pl.kind, J.sens, J.pl.block, J.pl.grid, J.pl.smem, st)
-                        : launch_fused<int>(p, J.pl.kind, J.sens, J.pl.block, J.pl.grid, J.pl.smem, st);
+            le = w == 8 ? launch_fused<long long>(p, J.pl.kind, J.gen, J.pl.block, J.pl.grid, J.pl.smem, st)
+                        : launch_fused<int>(p, J.pl.kind, J.gen, J.pl.block, J.pl.grid, J.pl.smem, st);
             launches = 1;
         } else {
             le = w == 8 ? launch_plain_init<long long>(p, st) : launch_plain_init<int>(p, st);
@@ -873,8 +875,8 @@ static tl_status run_batch(tl_batch_item* items, int n, cudaStream_t st) {
     bp.warp_slot_bytes = (int)wslot;
     bp.params_bytes = (int)spb;
     bp.wctr = reinterpret_cast<unsigned long long*>(B + o_wctr);
-    bool any_sens = false;
-    for (auto& J : jobs) any_sens |= J.sens;
+    bool any_sens = false;  // the general kernel: scores or compatibility switches in any item
+    for (auto& J : jobs) any_sens |= J.gen;
     const size_t smem = stage + (size_t)warps * (wslot + spb);
     int bps = 0;
     cudaError_t le = pop == 64 ? batch_occupancy<long long>(any_sens, 32 * warps, smem, &bps)
@@ -1407,7 +1409,7 @@ extern "C" tl_status tl_simulate_static(tl_model* m, const tl_run_cfg* cfg, tl_r
     if (ps != TL_OK) return ps;
     TLC(cudaSetDevice(m->d.device));
     cudaStream_t st = (cudaStream_t)cfg->stream;
-    ps = make_plan(m, cfg->variant, cfg->block_threads, false, J.compat_stoich,
+    ps = make_plan(m, cfg->variant, cfg->block_threads, J.gen, J.compat_stoich,
                    (cfg->flags & TL_FLAG_NO_STAGE) != 0, J.total, J.pl);
     if (ps != TL_OK) return ps;
     Carver c;
@@ -1424,8 +1426,8 @@ extern "C" tl_status tl_simulate_static(tl_model* m, const tl_run_cfg* cfg, tl_r
     ps = job_bind(J, reinterpret_cast<unsigned char*>(base), st);  // clears the counters
     if (ps != TL_OK) return ps;
     const auto tk = std::chrono::steady_clock::now();
-    cudaError_t le = J.w == 8 ? launch_fused<long long>(J.p, J.pl.kind, false, J.pl.block, J.pl.grid, J.pl.smem, st)
-                              : launch_fused<int>(J.p, J.pl.kind, false, J.pl.block, J.pl.grid, J.pl.smem, st);
+    cudaError_t le = J.w == 8 ? launch_fused<long long>(J.p, J.pl.kind, J.gen, J.pl.block, J.pl.grid, J.pl.smem, st)
+                              : launch_fused<int>(J.p, J.pl.kind, J.gen, J.pl.block, J.pl.grid, J.pl.smem, st);
     if (le != cudaSuccess) return cuda_fail(le, "simulation launch");
     ps = job_reduce(J, st);
     if (ps != TL_OK) return ps;

@@ -295,16 +295,19 @@ TL_D int poisson_reference(float mu, Rng& rng) {
 // >= 10, or the reference's sampler is asked for), out of line: it is the
 // rare path of a leap, and keeping it out of the unrolled channel loop keeps
 // the hot loop small in the instruction cache.
+// REFS: the reference's sampler can be asked for (compatibility builds).
+template <bool REFS>
 TL_D int poisson_rare_inline(float mu, float q, uint32_t j, uint32_t step, uint32_t r, uint32_t set, uint32_t k0,
                              uint32_t k1, int refs) {
     ChanRng rng;
     rng.init(j, step, r, set, k0, k1);
-    if (refs) return poisson_reference(mu, rng);
+    if (REFS && refs) return poisson_reference(mu, rng);
     return poisson_tail2(mu, q, rng);
 }
+template <bool REFS>
 static __device__ __noinline__ int poisson_rare(float mu, float q, uint32_t j, uint32_t step, uint32_t r,
                                                 uint32_t set, uint32_t k0, uint32_t k1, int refs) {
-    return poisson_rare_inline(mu, q, j, step, r, set, k0, k1, refs);
+    return poisson_rare_inline<REFS>(mu, q, j, step, r, set, k0, k1, refs);
 }
 
 // ---------------------------------------------------------------------------
@@ -686,6 +689,12 @@ struct RState {
 };
 
 TL_HD bool flag(unsigned f, unsigned b) { return (f & b) != 0; }
+// A reference-compatibility switch: compiled out of the kernels built
+// without them (COMPAT = false), read at run time otherwise.
+template <bool COMPAT>
+TL_D bool cflag(unsigned f, unsigned b) {
+    return COMPAT && (f & b) != 0;
+}
 
 template <class TimeT>
 TL_D TimeT grid_time(const SimParams& p, double T, int k) {
@@ -698,10 +707,10 @@ TL_D TimeT grid_time(const SimParams& p, double T, int k) {
 // ---------------------------------------------------------------------------
 
 // Propensities of all channels into a[] (sign = critical); lane partial sums.
-template <class Grp, class Pop>
+template <class Grp, class Pop, bool COMPAT = true>
 TL_D void pass_props(const Grp& g, const SimParams& p, const MView& mv, const float* rate,
                      const Pop* x, float* a, float& pa, float& pac) {
-    const bool cc = flag(p.flags, TL_FLAG_COMPAT_CRIT);
+    const bool cc = cflag<COMPAT>(p.flags, TL_FLAG_COMPAT_CRIT);
     float s = 0.f, sc = 0.f;
     for (int j = g.rank(); j < p.M; j += g.size()) {
         float aj;
@@ -717,10 +726,10 @@ TL_D void pass_props(const Grp& g, const SimParams& p, const MView& mv, const fl
 }
 
 // CGP bound of species i from its CSR row; optional moments out.
-template <class Pop>
+template <class Pop, bool COMPAT = true>
 TL_D float species_bound(const SimParams& p, const MView& mv, const Pop* x, const float* a, int i,
                          float mu, float s2) {
-    const bool cg = flag(p.flags, TL_FLAG_COMPAT_G);
+    const bool cg = cflag<COMPAT>(p.flags, TL_FLAG_COMPAT_G);
     const float xi = popf(x[i]);
     float gi;
     if (cg) {
@@ -736,10 +745,10 @@ TL_D float species_bound(const SimParams& p, const MView& mv, const Pop* x, cons
     return fminf(b1, b2);
 }
 
-template <bool OUT, class Grp, class Pop>
+template <bool OUT, class Grp, class Pop, bool COMPAT = true>
 TL_D float pass_tau(const Grp& g, const SimParams& p, const MView& mv, const Pop* x, const float* a,
                     float* mu_out, float* s2_out) {
-    const bool all_rows = flag(p.flags, TL_FLAG_COMPAT_STOICH);
+    const bool all_rows = cflag<COMPAT>(p.flags, TL_FLAG_COMPAT_STOICH);
     float tmin = kInfF;
     bool done = false;
     if constexpr (Grp::kWidth == 0) {
@@ -769,7 +778,7 @@ TL_D float pass_tau(const Grp& g, const SimParams& p, const MView& mv, const Pop
                     mu_out[i] = mu;
                     s2_out[i] = s2;
                 }
-                if (all_rows || mv.gkind[i] != 0) tmin = fminf(tmin, species_bound<Pop>(p, mv, x, a, i, mu, s2));
+                if (all_rows || mv.gkind[i] != 0) tmin = fminf(tmin, species_bound<Pop, COMPAT>(p, mv, x, a, i, mu, s2));
             }
         }
       }
@@ -794,7 +803,7 @@ TL_D float pass_tau(const Grp& g, const SimParams& p, const MView& mv, const Pop
                 mu_out[i] = mu;
                 s2_out[i] = s2;
             }
-            if (all_rows || mv.gkind[i] != 0) tmin = fminf(tmin, species_bound<Pop>(p, mv, x, a, i, mu, s2));
+            if (all_rows || mv.gkind[i] != 0) tmin = fminf(tmin, species_bound<Pop, COMPAT>(p, mv, x, a, i, mu, s2));
         }
     }
     return g.minf(tmin);
@@ -919,10 +928,10 @@ TL_D void record_point(const Grp& g, const SimParams& p, const Pop* x, Pop* samp
 // Poisson firing counts of one leap (model.cu:458-549), written over a[] as
 // ints.  A thread takes four consecutive channels at a time so that they
 // share one Philox block for their first uniforms.
-template <class Grp>
+template <class Grp, bool COMPAT = true>
 TL_D void pass_fire(const Grp& g, const SimParams& p, float* a, float tauf, int jc, uint32_t step, uint32_t r,
                     uint32_t set) {
-    const bool refs = flag(p.flags, TL_FLAG_COMPAT_POISSON);
+    const bool refs = cflag<COMPAT>(p.flags, TL_FLAG_COMPAT_POISSON);
     const bool vec = (reinterpret_cast<uintptr_t>(a) & 15) == 0;
     int* kk = reinterpret_cast<int*>(a);
     for (int g4 = g.rank(); 4 * g4 < p.M; g4 += g.size()) {
@@ -977,9 +986,9 @@ TL_D void pass_fire(const Grp& g, const SimParams& p, float* a, float tauf, int 
                     // thread groups inline the rare draw (their loop is per
                     // thread anyway); warp / CTA groups call it out of line
                     if constexpr (Grp::kWidth == 1)
-                        k = poisson_rare_inline(mu, q, (uint32_t)j, step, r, set, p.k0, p.k1, refs ? 1 : 0);
+                        k = poisson_rare_inline<COMPAT>(mu, q, (uint32_t)j, step, r, set, p.k0, p.k1, refs ? 1 : 0);
                     else
-                        k = poisson_rare(mu, q, (uint32_t)j, step, r, set, p.k0, p.k1, refs ? 1 : 0);
+                        k = poisson_rare<COMPAT>(mu, q, (uint32_t)j, step, r, set, p.k0, p.k1, refs ? 1 : 0);
                 }
                 kv[e] = k;
             }
@@ -998,7 +1007,7 @@ TL_D void pass_fire(const Grp& g, const SimParams& p, float* a, float tauf, int 
 // One step of one realization: a tau-leap (with rejection + halving) or a
 // block of direct-method steps (model.cu:301-413).
 // ---------------------------------------------------------------------------
-template <class Grp, class Pop, class TimeT, bool SENS>
+template <class Grp, class Pop, class TimeT, bool SENS, bool COMPAT = true>
 TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& s, int set, uint32_t r,
                   Pop* samp, float* score, RState<TimeT>& st) {
     const float* rate = p.rates + (size_t)set * p.M;
@@ -1006,7 +1015,7 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
     const unsigned f = p.flags;
 
     float pa, pac;
-    pass_props<Grp, Pop>(g, p, mv, rate, s.x, s.a, pa, pac);
+    pass_props<Grp, Pop, COMPAT>(g, p, mv, rate, s.x, s.a, pa, pac);
     g.sync();
     const float a0f = g.sumf(pa);  // FP32: only the branch test and tau2 use it
     if (!(a0f > 0.f)) {
@@ -1016,13 +1025,13 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
         st.done = 1;
         return;
     }
-    float tau1 = pass_tau<false, Grp, Pop>(g, p, mv, s.x, s.a, nullptr, nullptr);
+    float tau1 = pass_tau<false, Grp, Pop, COMPAT>(g, p, mv, s.x, s.a, nullptr, nullptr);
 
     if (tau1 * a0f < p.ssa_factor) {
         // ---- direct-method block (CGP 2006 step 2; model.cu:334-345) ----
         for (int q = 0; q < p.ssa_block; ++q) {
             if (q > 0) {
-                pass_props<Grp, Pop>(g, p, mv, rate, s.x, s.a, pa, pac);
+                pass_props<Grp, Pop, COMPAT>(g, p, mv, rate, s.x, s.a, pa, pac);
                 g.sync();
             }
             // total for the cumulative search: FP64 over the lane partials
@@ -1043,7 +1052,7 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
             const int j = select_channel<Grp, TimeT>(g, p, s.a, pa, target, 0);
             // the waiting time in FP32 (FP64 keeps only the time sum)
             const float ex = -logf(u01f(w.x));
-            const TimeT dt = (TimeT)(flag(f, TL_FLAG_COMPAT_TAU2) ? ex / fabsf(s.a[j]) : ex / (float)a0);
+            const TimeT dt = (TimeT)(cflag<COMPAT>(f, TL_FLAG_COMPAT_TAU2) ? ex / fabsf(s.a[j]) : ex / (float)a0);
             while (st.kpt <= p.n_int && st.t + dt >= grid_time<TimeT>(p, T, st.kpt))
                 record_point<Grp, Pop>(g, p, s.x, samp, st.kpt++);
             if (st.kpt > p.n_int) {
@@ -1067,7 +1076,7 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
                 }
             }
             g.sync();
-            if (!flag(f, TL_FLAG_COMPAT_SSA) && j >= 0) {
+            if (!cflag<COMPAT>(f, TL_FLAG_COMPAT_SSA) && j >= 0) {
                 const int e = mv.cp[j + 1];
                 for (int q2 = mv.cp[j] + g.rank(); q2 < e; q2 += g.size()) {
                     const int pk = mv.rv[q2];
@@ -1096,7 +1105,7 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
         int jc = -1;
         float tau2 = kInfF;
         if (a0cf > 0.f) {
-            if (flag(f, TL_FLAG_COMPAT_TAU2)) {
+            if (cflag<COMPAT>(f, TL_FLAG_COMPAT_TAU2)) {
                 const TimeT a0c = (TimeT)g.sumd((double)pac);
                 jc = select_channel<Grp, TimeT>(g, p, s.a, pac, (TimeT)u01d(w.z, w.w) * a0c, 1);
                 tau2 = -logf(u01f(w.x)) / fabsf(s.a[jc]);
@@ -1118,7 +1127,7 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
             jc = select_channel<Grp, TimeT>(g, p, s.a, pac, (TimeT)u01d(w.z, w.w) * a0c, 1);
         }
         if (!fire) jc = -1;
-        pass_fire<Grp>(g, p, s.a, tauf, jc, st.step, r, (uint32_t)set);
+        pass_fire<Grp, COMPAT>(g, p, s.a, tauf, jc, st.step, r, (uint32_t)set);
         int* kk = reinterpret_cast<int*>(s.a);
         g.sync();
         bool ovf = false;
@@ -1135,7 +1144,7 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
         st.rej++;
         tau1 *= 0.5f;
         g.sync();
-        pass_props<Grp, Pop>(g, p, mv, rate, s.x, s.a, pa, pac);
+        pass_props<Grp, Pop, COMPAT>(g, p, mv, rate, s.x, s.a, pa, pac);
         g.sync();
         if (attempt >= 64) {
             if (g.leader()) atomicOr((unsigned*)(p.ctr + 5), kErrHalving);
@@ -1146,7 +1155,7 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
     }
     if (SENS && score) {
         // score_j += (k_j - a_j*tau)/c_j with a_j recomputed from the old state
-        const bool cc = flag(f, TL_FLAG_COMPAT_CRIT);
+        const bool cc = cflag<COMPAT>(f, TL_FLAG_COMPAT_CRIT);
         const float tauf = tau_used;
         const int* kk = reinterpret_cast<const int*>(s.a);
         for (int m = g.rank(); m < p.M; m += g.size()) {
