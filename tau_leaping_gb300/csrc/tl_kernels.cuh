@@ -173,17 +173,31 @@ TL_D void run_realization(const Grp& g, const SimParams& p, const MView& mv, Slo
 // ---------------------------------------------------------------------------
 // Fused persistent kernel.
 // ---------------------------------------------------------------------------
-// Thread and warp groups launch at most 256 threads per CTA and ask the
-// compiler for TL_WARP_MINB resident CTAs per SM (register budget
-// 65536 / (256 * TL_WARP_MINB) per thread); CTA groups use up to 1024.
+// Thread, sub-warp and warp groups launch at most 256 threads per CTA and
+// ask the compiler for a number of resident CTAs per SM, which sets the
+// register budget 65536 / (256 * n) per thread: TL_THREAD_MINB for thread
+// groups, TL_WARP_MINB for the others.  CTA groups use up to 1024 threads.
+// Defaults from sweeps on GB300: warp groups run best at 5 CTAs (51
+// registers; 4 and 6 were 9 % slower on the toy network), thread groups
+// at 3 (85 registers; 8 % faster than 4 on the dimer).
 #ifndef TL_WARP_MINB
-#define TL_WARP_MINB 4
+#define TL_WARP_MINB 5
+#endif
+#ifndef TL_THREAD_MINB
+#define TL_THREAD_MINB 3
+#endif
+// The batch kernel (thread and warp units, scores on) at 2 CTAs per SM
+// (128 registers): 1 gives 160 registers and one CTA per SM (-37 %), 4 and
+// 5 spill (-24 %, -22 %).
+#ifndef TL_BATCH_MINB
+#define TL_BATCH_MINB 2
 #endif
 // GEN: the general kernel, with the likelihood-ratio scores and the
 // reference-compatibility switches; the other build has neither (about 6 %
 // faster: smaller code, fewer registers spilled).
 template <int KIND, class Pop, bool GEN>
-__global__ void __launch_bounds__(KIND == 0 ? 1024 : 256, KIND == 0 ? 1 : TL_WARP_MINB) k_fused(SimParams p) {
+__global__ void __launch_bounds__(KIND == 0 ? 1024 : 256, KIND == 0 ? 1 : KIND == 1 ? TL_THREAD_MINB : TL_WARP_MINB)
+    k_fused(SimParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ __align__(8) unsigned long long mbar;
     __shared__ double red[34];
@@ -230,7 +244,7 @@ TL_D void add_counts(unsigned long long* ctr, long long nl, long long ns, long l
 }
 
 template <class Pop, bool GEN>
-__global__ void __launch_bounds__(256) k_batch(BatchParams bp) {
+__global__ void __launch_bounds__(256, TL_BATCH_MINB) k_batch(BatchParams bp) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ __align__(8) unsigned long long mbar;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
