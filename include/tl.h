@@ -357,8 +357,10 @@ tl_status tl_philox(const uint32_t *ctr, const uint32_t *key, int32_t n,
                     uint32_t *out);
 
 /*
- * Poisson sampler on the device: out[i] ~ Poisson(mean[i]) using the uniform
- * stream (i, step, 0, 0) under seed; compat != 0 selects the reference's
+ * Poisson sampler on the device: out[i] ~ Poisson(mean[i]), drawn exactly as
+ * the simulation draws channel i of realization 0 in step `step` (the first
+ * word from the block shared by channels 4(i/4)..4(i/4)+3, then the private
+ * stream (i, step, 0, b)) under seed; compat != 0 selects the reference's
  * sampler.  For distribution tests.
  */
 tl_status tl_poisson(const float *mean, int32_t n, uint64_t seed,
