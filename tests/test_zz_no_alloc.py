@@ -33,6 +33,17 @@ def test_static_entry_matches_simulate_on_two_calls_in_a_row():
     assert np.allclose(dgot.mean, dref.mean, rtol=1e-12, atol=0)
 
 
+def test_static_entry_with_compatibility_switches_matches_simulate():
+    """A run with reference-compatibility switches takes the general kernel
+    build on both entry points."""
+    m = Model.generate("toy", n_species=32, n_channels=64, seed=4, x0_max=3000)
+    kw = dict(t_final=0.005, n=2000, seed=5, tracked=[0, 1], flags=_ffi.FLAG_COMPAT_REFERENCE)
+    ref = m.simulate(**kw)
+    got = m.simulate_static(**kw)
+    assert np.allclose(got.mean, ref.mean, rtol=1e-12, atol=0)
+    assert (got.leaps, got.ssa_steps, got.rejections) == (ref.leaps, ref.ssa_steps, ref.rejections)
+
+
 def test_static_entry_limits():
     m = Model.generate("dimer", x0_min=500, x0_max=500)
     with pytest.raises(_ffi.TLError) as e:      # tables not resident yet
