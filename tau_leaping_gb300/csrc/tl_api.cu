@@ -702,7 +702,7 @@ static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad
                 }
             }
             unsigned long long* hdone = nullptr;
-            cudaMallocHost(&hdone, 8);
+            if (le == cudaSuccess) le = cudaMallocHost(&hdone, 8);
             while (le == cudaSuccess) {
                 if (gexec) {
                     le = cudaGraphLaunch(gexec, st);
@@ -728,7 +728,7 @@ static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad
                 }
             }
             if (gexec) cudaGraphExecDestroy(gexec);
-            cudaFreeHost(hdone);
+            if (hdone) cudaFreeHost(hdone);
             if (le == cudaSuccess) le = launch_plain_tally(p, st);
             ++launches;
         }
