@@ -177,7 +177,11 @@ struct Plan {
     int stage = 0;      // staged bytes (0 = constants read through L1/L2)
     int variant = TL_VARIANT_WARP;
     bool row_warp = false;
+    bool gslot = false;  // CTA groups: the slot lives in global memory
 };
+
+// The kernel a plan launches (CTA groups with global slots are their own build).
+static int launch_kind(const Plan& pl) { return pl.gslot ? kKindCtaGlobal : pl.kind; }
 
 // Autotuner, heuristic part: the group width follows the model size.
 //  * a handful of channels: one realization per thread (all lanes busy on
@@ -244,18 +248,25 @@ static tl_status make_plan(const tl_model* m, int variant, int block_req, bool g
         groups_per_block = pl.block / pl.kind;
     }
     if ((size_t)groups_per_block * sb > (size_t)smax) {
-        set_last_error("model too large for the shared-memory slot of this variant");
-        return TL_ERR_UNSUPPORTED;
+        if (pl.kind != 0) {
+            set_last_error("model too large for the shared-memory slot of this variant");
+            return TL_ERR_UNSUPPORTED;
+        }
+        // one realization's state exceeds shared memory: CTA groups keep it
+        // in global memory (one slot per CTA, served from L2)
+        pl.gslot = true;
     }
     // chain-sized CTA groups leave the tables in L1/L2 (staging them would
     // cost more shared memory than the realization itself)
     const bool stage_ok = !(autov && pl.kind == 0 && sb <= 64 * 1024);
-    pl.stage = (stage_ok && (size_t)groups_per_block * sb + (size_t)stage <= (size_t)smax) ? stage : 0;
-    pl.smem = (size_t)pl.stage + (size_t)groups_per_block * sb;
+    const size_t slot_smem = pl.gslot ? 0 : (size_t)groups_per_block * sb;
+    pl.stage = (stage_ok && slot_smem + (size_t)stage <= (size_t)smax) ? stage : 0;
+    pl.smem = (size_t)pl.stage + slot_smem;
     pl.row_warp = pl.kind == 0 && m->h.max_row > 32;
     int bps = 0;
-    cudaError_t e = m->h.pop_bits == 64 ? fused_occupancy<long long>(pl.kind, gen, pl.block, pl.smem, &bps)
-                                        : fused_occupancy<int>(pl.kind, gen, pl.block, pl.smem, &bps);
+    const int lk = pl.gslot ? kKindCtaGlobal : pl.kind;
+    cudaError_t e = m->h.pop_bits == 64 ? fused_occupancy<long long>(lk, gen, pl.block, pl.smem, &bps)
+                                        : fused_occupancy<int>(lk, gen, pl.block, pl.smem, &bps);
     if (e != cudaSuccess) return cuda_fail(e, "occupancy");
     if (bps < 1) {
         set_last_error("the launch does not fit an SM");
@@ -299,7 +310,7 @@ struct Job {
     std::vector<double> htf;
     Plan pl;
     size_t o_rates = 0, o_tf = 0, o_tr = 0, o_samp = 0, o_sc = 0, o_ctr = 0, o_mean = 0, o_sd = 0, o_grad = 0,
-           o_gse = 0, o_gm = 0, o_ps = 0, o_pslot = 0, o_aall = 0;
+           o_gse = 0, o_gm = 0, o_ps = 0, o_pslot = 0, o_aall = 0, o_gslot = 0;
     RunBuffers rb;
     SimParams p{};
     std::vector<unsigned char> hs;
@@ -395,6 +406,7 @@ static void job_layout(Job& J, Carver& c) {
     J.o_ps = J.plain ? c.take((size_t)J.total * 64) : 0;
     J.o_pslot = J.plain ? c.take((size_t)J.total * 2 * al16((size_t)N * J.w)) : 0;
     J.o_aall = J.plain ? c.take((size_t)J.total * M * 4) : 0;
+    J.o_gslot = (!J.plain && J.pl.gslot) ? c.take((size_t)J.pl.grid * slot_bytes(J.m)) : 0;
 }
 
 static tl_status job_bind(Job& J, unsigned char* B, cudaStream_t st) {
@@ -458,6 +470,7 @@ static tl_status job_bind(Job& J, unsigned char* B, cudaStream_t st) {
     p.off_rv = m->d.off_rv;
     p.slot_bytes = (int)slot_bytes(m);
     p.row_warp = J.pl.row_warp ? 1 : 0;
+    p.gslots = J.pl.gslot ? B + J.o_gslot : nullptr;
     p.ctr = rb.ctr;
     p.pstate = rb.pstate;
     p.pslots = rb.pslots;
@@ -560,6 +573,9 @@ static double ms_since(std::chrono::steady_clock::time_point t0) {
 // prefix of the sample buffer, which the real run then overwrites.
 static tl_status autotune_measure(Job& J, cudaStream_t st) {
     tl_model* m = J.m;
+    const bool planned_gslot = J.pl.gslot;
+    const int planned_grid = J.pl.grid;
+    unsigned char* const planned_gslots = J.p.gslots;
     // the best plan depends on how many realizations fill the GPU: key the
     // cache by the ensemble size (power-of-two bucket) as well
     int bucket = 0;
@@ -595,12 +611,15 @@ static tl_status autotune_measure(Job& J, cudaStream_t st) {
             Plan pl;
             if (make_plan(m, c.variant, c.block, J.gen, J.compat_stoich, c.nostage, trial, pl) != TL_OK) continue;
             if (c.variant == TL_VARIANT_THREAD && c.block != pl.block) continue;
+            // global slots exist for the launch the heuristic planned
+            if (pl.gslot && (!planned_gslot || pl.grid > planned_grid)) continue;
             tp.stage_bytes = pl.stage;
             tp.row_warp = pl.row_warp ? 1 : 0;
+            tp.gslots = pl.gslot ? planned_gslots : nullptr;
             if (cudaMemsetAsync(tp.ctr, 0, 64, st) != cudaSuccess) break;
             cudaEventRecord(e0, st);
-            cudaError_t le = J.w == 8 ? launch_fused<long long>(tp, pl.kind, J.gen, pl.block, pl.grid, pl.smem, st)
-                                      : launch_fused<int>(tp, pl.kind, J.gen, pl.block, pl.grid, pl.smem, st);
+            cudaError_t le = J.w == 8 ? launch_fused<long long>(tp, launch_kind(pl), J.gen, pl.block, pl.grid, pl.smem, st)
+                                      : launch_fused<int>(tp, launch_kind(pl), J.gen, pl.block, pl.grid, pl.smem, st);
             cudaEventRecord(e1, st);
             if (le != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
                 cudaGetLastError();
@@ -628,8 +647,16 @@ static tl_status autotune_measure(Job& J, cudaStream_t st) {
     tl_status ps = make_plan(m, m->tuned_variant, m->tuned_block, J.gen, J.compat_stoich, m->tuned_nostage != 0,
                              J.total, J.pl);
     if (ps != TL_OK) return ps;
+    if (J.pl.gslot && (!planned_gslot || J.pl.grid > planned_grid)) {
+        // a cached global-slot plan that needs more slots than were laid out:
+        // keep the planned launch
+        ps = make_plan(m, TL_VARIANT_AUTO, 0, J.gen, J.compat_stoich, (J.cfg->flags & TL_FLAG_NO_STAGE) != 0,
+                       J.total, J.pl);
+        if (ps != TL_OK) return ps;
+    }
     J.p.stage_bytes = J.pl.stage;
     J.p.row_warp = J.pl.row_warp ? 1 : 0;
+    J.p.gslots = J.pl.gslot ? planned_gslots : nullptr;
     return TL_OK;
 }
 
@@ -676,8 +703,8 @@ static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad
     cudaError_t le = cudaEventRecord(e0, st);
     if (le == cudaSuccess) {
         if (!J.plain) {
-            le = w == 8 ? launch_fused<long long>(p, J.pl.kind, J.gen, J.pl.block, J.pl.grid, J.pl.smem, st)
-                        : launch_fused<int>(p, J.pl.kind, J.gen, J.pl.block, J.pl.grid, J.pl.smem, st);
+            le = w == 8 ? launch_fused<long long>(p, launch_kind(J.pl), J.gen, J.pl.block, J.pl.grid, J.pl.smem, st)
+                        : launch_fused<int>(p, launch_kind(J.pl), J.gen, J.pl.block, J.pl.grid, J.pl.smem, st);
             launches = 1;
         } else {
             le = w == 8 ? launch_plain_init<long long>(p, st) : launch_plain_init<int>(p, st);
@@ -1426,8 +1453,8 @@ extern "C" tl_status tl_simulate_static(tl_model* m, const tl_run_cfg* cfg, tl_r
     ps = job_bind(J, reinterpret_cast<unsigned char*>(base), st);  // clears the counters
     if (ps != TL_OK) return ps;
     const auto tk = std::chrono::steady_clock::now();
-    cudaError_t le = J.w == 8 ? launch_fused<long long>(J.p, J.pl.kind, J.gen, J.pl.block, J.pl.grid, J.pl.smem, st)
-                              : launch_fused<int>(J.p, J.pl.kind, J.gen, J.pl.block, J.pl.grid, J.pl.smem, st);
+    cudaError_t le = J.w == 8 ? launch_fused<long long>(J.p, launch_kind(J.pl), J.gen, J.pl.block, J.pl.grid, J.pl.smem, st)
+                              : launch_fused<int>(J.p, launch_kind(J.pl), J.gen, J.pl.block, J.pl.grid, J.pl.smem, st);
     if (le != cudaSuccess) return cuda_fail(le, "simulation launch");
     ps = job_reduce(J, st);
     if (ps != TL_OK) return ps;

@@ -645,6 +645,8 @@ struct SimParams {
     int off_chan, off_gkind, off_perm, off_rp, off_vc, off_cp, off_rv;  // byte offsets (net)
     int slot_bytes;     // per group
     int row_warp;       // CTA groups: one warp per species row (long rows)
+    unsigned char* gslots;  // CTA groups whose slot exceeds shared memory:
+                            // one slot per CTA in global memory (else null)
     unsigned long long* ctr; // [0] work, [1] leaps, [2] ssa, [3] rejections,
                              // [4] truncated, [5] error bits, [6] done count
     // plain form state

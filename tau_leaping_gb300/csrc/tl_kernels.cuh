@@ -195,7 +195,10 @@ TL_D void run_realization(const Grp& g, const SimParams& p, const MView& mv, Slo
 // GEN: the general kernel, with the likelihood-ratio scores and the
 // reference-compatibility switches; the other build has neither (about 6 %
 // faster: smaller code, fewer registers spilled).
-template <int KIND, class Pop, bool GEN>
+// GSLOT (CTA groups only): each CTA's slot lives in global memory, for
+// realizations whose state exceeds shared memory.  A separate build, so
+// that the shared-memory kernels keep shared-memory addressing.
+template <int KIND, class Pop, bool GEN, bool GSLOT = false>
 __global__ void __launch_bounds__(KIND == 0 ? 1024 : 256, KIND == 0 ? 1 : KIND == 1 ? TL_THREAD_MINB : TL_WARP_MINB)
     k_fused(SimParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -214,6 +217,7 @@ __global__ void __launch_bounds__(KIND == 0 ? 1024 : 256, KIND == 0 ? 1 : KIND =
         slots = smem + p.stage_bytes;
     }
     const Grp g = GroupOf<KIND>::make(red);
+    if constexpr (GSLOT) slots = p.gslots + (size_t)blockIdx.x * (size_t)p.slot_bytes;
     Slot<Pop> s = carve_slot<Pop>(slots + (size_t)GroupOf<KIND>::index() * p.slot_bytes, p);
     const long long total = p.R * (long long)p.S;
     long long nl = 0, ns = 0, nr = 0, ntr = 0;

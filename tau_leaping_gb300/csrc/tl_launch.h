@@ -8,7 +8,9 @@ namespace tl {
 
 struct SimParams;
 
-// kind: 1 = thread, 32 = warp, 0 = CTA, 2/4/8/16 = lanes per realization.
+// kind: 1 = thread, 32 = warp, 0 = CTA, 2/4/8/16 = lanes per realization,
+// kKindCtaGlobal = CTA with its slot in global memory.
+constexpr int kKindCtaGlobal = 64;
 template <class Pop>
 cudaError_t launch_fused(const SimParams& p, int kind, bool gen, int block, int grid, size_t smem,
                          cudaStream_t st);

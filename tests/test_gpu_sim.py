@@ -197,6 +197,22 @@ def test_colloid_full_config_within_1pct_of_fp64_oracle(capsys):
     assert np.all(rel_v <= 0.01 + 4 * se_v), rel_v.max()
 
 
+def test_state_larger_than_shared_memory_runs_from_global_slots():
+    """Colloidal aggregation with 400 species: 80 000 channels, 320 KB of
+    propensities per realization, more than a CTA's shared memory.  CTA
+    groups then keep each realization's state in global memory."""
+    m = Model.generate("colloid", n_species=400)
+    assert m.n_channels == 80000
+    g = m.simulate(0.002, 256, seed=4, tracked=[0, 1, 9], keep_samples=True)
+    assert g.variant == _ffi.VARIANT_CTA and g.leaps > 0
+    o = ora.OracleModel.from_desc(m.desc())
+    r = o.simulate(0.002, 256, seed=5, tracked=[0, 1, 9], threads=8)
+    compare_final(g.samples[0, :, -1, :], r["samples"][0, :, -1, :], "colloid-400 global slots")
+    # the same realizations again: deterministic
+    h = m.simulate(0.002, 256, seed=4, tracked=[0, 1, 9], keep_samples=True)
+    assert np.array_equal(g.samples, h.samples)
+
+
 def test_measured_autotuner_picks_a_plan_and_caches_it():
     m = Model.generate("toy", n_species=32, n_channels=64, seed=4, x0_max=3000)
     o = ora.OracleModel.from_desc(m.desc())
