@@ -356,7 +356,8 @@ def e2e(args, wl, m, R, T, stream, sptr):
         dt = time.perf_counter() - t0
         tot += dt
         steps += r.leaps + r.ssa_steps
-    return {"value": steps / tot, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+    return {"value": steps / tot, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "steps": n, "timing": "host wall clock around model upload + tl_simulate + statistics read-back"}
 
 
 def cpu_baseline(args, wl, m, R, budget_s: float = 12.0, check_gpu: bool = False):
