@@ -149,9 +149,10 @@ static MView global_view(const tl_model* m, bool raw_mu, bool raw_update) {
     return v;
 }
 
-static size_t slot_bytes(const tl_model* m) {
+// One group's slot: x, x' and a[]; scored runs add the firing counts.
+static size_t slot_bytes(const tl_model* m, bool sens = false) {
     const size_t w = m->h.pop_bits == 64 ? 8 : 4;
-    return al16((size_t)m->h.N * w) * 2 + al16((size_t)m->h.M * 4);
+    return al16((size_t)m->h.N * w) * 2 + al16((size_t)m->h.M * 4) * (sens ? 2 : 1);
 }
 
 static int max_smem_optin() {
@@ -203,7 +204,7 @@ static int heuristic_variant(const tl_model* m, size_t sb) {
 
 static tl_status make_plan(const tl_model* m, int variant, int block_req, bool gen, bool compat_stoich,
                            bool no_stage, long long total, Plan& pl) {
-    const size_t sb = slot_bytes(m);
+    const size_t sb = slot_bytes(m, gen);
     const int smax = max_smem_optin() - 2048;
     const int stage = (compat_stoich || no_stage) ? 0 : m->d.stage_bytes;
     const bool autov = variant == TL_VARIANT_AUTO;
@@ -406,7 +407,7 @@ static void job_layout(Job& J, Carver& c) {
     J.o_ps = J.plain ? c.take((size_t)J.total * 64) : 0;
     J.o_pslot = J.plain ? c.take((size_t)J.total * 2 * al16((size_t)N * J.w)) : 0;
     J.o_aall = J.plain ? c.take((size_t)J.total * M * 4) : 0;
-    J.o_gslot = (!J.plain && J.pl.gslot) ? c.take((size_t)J.pl.grid * slot_bytes(J.m)) : 0;
+    J.o_gslot = (!J.plain && J.pl.gslot) ? c.take((size_t)J.pl.grid * slot_bytes(J.m, J.gen)) : 0;
 }
 
 static tl_status job_bind(Job& J, unsigned char* B, cudaStream_t st) {
@@ -468,7 +469,7 @@ static tl_status job_bind(Job& J, unsigned char* B, cudaStream_t st) {
     p.off_vc = m->d.off_vc;
     p.off_cp = m->d.off_cp;
     p.off_rv = m->d.off_rv;
-    p.slot_bytes = (int)slot_bytes(m);
+    p.slot_bytes = (int)slot_bytes(m, J.gen);
     p.row_warp = J.pl.row_warp ? 1 : 0;
     p.gslots = J.pl.gslot ? B + J.o_gslot : nullptr;
     p.ctr = rb.ctr;
@@ -820,7 +821,8 @@ static tl_status run_batch(tl_batch_item* items, int n, cudaStream_t st) {
     for (int i = 0; i < n; ++i) {
         const tl_model* m = jobs[(size_t)i].m;
         lane[(size_t)i] = (m->h.M <= 16 && m->h.N <= 16) ? 1 : 0;
-        const size_t need = lane[(size_t)i] ? 32 * slot_bytes(m) : slot_bytes(m);
+        const size_t sbi = slot_bytes(m, jobs[(size_t)i].gen);
+        const size_t need = lane[(size_t)i] ? 32 * sbi : sbi;
         wslot = std::max(wslot, need);
         Plan& pl = jobs[(size_t)i].pl;
         pl.variant = lane[(size_t)i] ? TL_VARIANT_THREAD : TL_VARIANT_WARP;

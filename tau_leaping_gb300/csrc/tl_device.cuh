@@ -677,7 +677,9 @@ template <class Pop>
 struct Slot {
     Pop* x;
     Pop* xn;   // next state of the update
-    float* a;  // propensity (sign bit = critical); holds int firing counts after the Poisson pass
+    float* a;  // propensity (sign bit = critical)
+    int* k;    // firing counts of the leap: over a[] unless the run keeps
+               // likelihood-ratio scores, which read a[] after the leap
 };
 
 template <class TimeT>
@@ -931,11 +933,10 @@ TL_D void record_point(const Grp& g, const SimParams& p, const Pop* x, Pop* samp
 // ints.  A thread takes four consecutive channels at a time so that they
 // share one Philox block for their first uniforms.
 template <class Grp, bool COMPAT = true>
-TL_D void pass_fire(const Grp& g, const SimParams& p, float* a, float tauf, int jc, uint32_t step, uint32_t r,
-                    uint32_t set) {
+TL_D void pass_fire(const Grp& g, const SimParams& p, const float* a, int* kk, float tauf, int jc, uint32_t step,
+                    uint32_t r, uint32_t set) {
     const bool refs = cflag<COMPAT>(p.flags, TL_FLAG_COMPAT_POISSON);
-    const bool vec = (reinterpret_cast<uintptr_t>(a) & 15) == 0;
-    int* kk = reinterpret_cast<int*>(a);
+    const bool vec = (reinterpret_cast<uintptr_t>(a) & 15) == 0 && (reinterpret_cast<uintptr_t>(kk) & 15) == 0;
     for (int g4 = g.rank(); 4 * g4 < p.M; g4 += g.size()) {
         const int j0 = 4 * g4;
         const bool full = vec && j0 + 3 < p.M;
@@ -1129,8 +1130,8 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
             jc = select_channel<Grp, TimeT>(g, p, s.a, pac, (TimeT)u01d(w.z, w.w) * a0c, 1);
         }
         if (!fire) jc = -1;
-        pass_fire<Grp, COMPAT>(g, p, s.a, tauf, jc, st.step, r, (uint32_t)set);
-        int* kk = reinterpret_cast<int*>(s.a);
+        pass_fire<Grp, COMPAT>(g, p, s.a, s.k, tauf, jc, st.step, r, (uint32_t)set);
+        int* kk = s.k;
         g.sync();
         bool ovf = false;
         const bool bad = pass_update<Grp, Pop>(g, p, mv, s.x, kk, s.xn, ovf);
@@ -1156,18 +1157,13 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
         }
     }
     if (SENS && score) {
-        // score_j += (k_j - a_j*tau)/c_j with a_j recomputed from the old state
-        const bool cc = cflag<COMPAT>(f, TL_FLAG_COMPAT_CRIT);
+        // score_j += (k_j - a_j*tau)/c_j with a_j of the pre-leap state, kept
+        // in a[] (the counts went to their own array in scored runs)
         const float tauf = tau_used;
-        const int* kk = reinterpret_cast<const int*>(s.a);
+        const int* kk = s.k;
         for (int m = g.rank(); m < p.M; m += g.size()) {
             const float c = __ldg(rate + m);
-            if (c > 0.f) {
-                float am;
-                bool cr;
-                propensity<Pop>(mv.chan[m], c, s.x, p.nc, cc, am, cr);
-                score[m] += ((float)kk[m] - am * tauf) / c;
-            }
+            if (c > 0.f) score[m] += ((float)kk[m] - fabsf(s.a[m]) * tauf) / c;
         }
     }
     g.sync();

@@ -102,6 +102,9 @@ TL_D Slot<Pop> carve_slot(unsigned char* base, const SimParams& p) {
     s.x = reinterpret_cast<Pop*>(base);
     s.xn = reinterpret_cast<Pop*>(base + xb);
     s.a = reinterpret_cast<float*>(base + 2 * xb);
+    // scored runs keep the counts apart (their slots hold M more ints)
+    s.k = p.scores ? reinterpret_cast<int*>(base + 2 * xb + (((size_t)p.M * 4 + 15) & ~(size_t)15))
+                   : reinterpret_cast<int*>(s.a);
     return s;
 }
 
@@ -355,6 +358,7 @@ __global__ void k_plain_step(SimParams p, float* a_all) {
         s.xn = t;
     }
     s.a = a_all + (size_t)w * p.M;
+    s.k = reinterpret_cast<int*>(s.a);
     Pop* const x_before = s.x;
     const int set = (int)(w / p.R);
     const uint32_t r = (uint32_t)(p.r_off + w - (long long)set * p.R);
