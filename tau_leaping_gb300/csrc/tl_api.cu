@@ -202,9 +202,9 @@ static int heuristic_variant(const tl_model* m, size_t sb) {
     return TL_VARIANT_CTA;
 }
 
-static tl_status make_plan(const tl_model* m, int variant, int block_req, bool gen, bool compat_stoich,
+static tl_status make_plan(const tl_model* m, int variant, int block_req, int mode, bool compat_stoich,
                            bool no_stage, long long total, Plan& pl) {
-    const size_t sb = slot_bytes(m, gen);
+    const size_t sb = slot_bytes(m, mode != kModeFast);
     const int smax = max_smem_optin() - 2048;
     const int stage = (compat_stoich || no_stage) ? 0 : m->d.stage_bytes;
     const bool autov = variant == TL_VARIANT_AUTO;
@@ -266,8 +266,8 @@ static tl_status make_plan(const tl_model* m, int variant, int block_req, bool g
     pl.row_warp = pl.kind == 0 && m->h.max_row > 32;
     int bps = 0;
     const int lk = pl.gslot ? kKindCtaGlobal : pl.kind;
-    cudaError_t e = m->h.pop_bits == 64 ? fused_occupancy<long long>(lk, gen, pl.block, pl.smem, &bps)
-                                        : fused_occupancy<int>(lk, gen, pl.block, pl.smem, &bps);
+    cudaError_t e = m->h.pop_bits == 64 ? fused_occupancy<long long>(lk, mode, pl.block, pl.smem, &bps)
+                                        : fused_occupancy<int>(lk, mode, pl.block, pl.smem, &bps);
     if (e != cudaSuccess) return cuda_fail(e, "occupancy");
     if (bps < 1) {
         set_last_error("the launch does not fit an SM");
@@ -305,7 +305,7 @@ struct Job {
     int S = 1, P = 2, K = 0;
     long long R = 1, total = 1;
     bool sens = false, keep = false, plain = false, compat_stoich = false;
-    bool gen = false;  // launch the general kernel (scores or compatibility switches)
+    int mode = kModeFast;  // the kernel build: scores and / or compatibility switches
     size_t w = 4;
     std::vector<float> hrates;
     std::vector<double> htf;
@@ -356,7 +356,7 @@ static tl_status job_prepare(Job& J) {
     J.K = cfg->n_tracked;
     J.total = J.R * J.S;
     J.sens = J.grad != nullptr;
-    J.gen = J.sens || (cfg->flags & TL_FLAG_COMPAT_REFERENCE) != 0;
+    J.mode = (cfg->flags & TL_FLAG_COMPAT_REFERENCE) ? kModeGeneral : J.sens ? kModeScores : kModeFast;
     J.keep = (cfg->flags & TL_FLAG_KEEP_SAMPLES) != 0;
     J.plain = cfg->variant == TL_VARIANT_PLAIN;
     J.compat_stoich = (cfg->flags & TL_FLAG_COMPAT_STOICH) != 0;
@@ -407,7 +407,7 @@ static void job_layout(Job& J, Carver& c) {
     J.o_ps = J.plain ? c.take((size_t)J.total * 64) : 0;
     J.o_pslot = J.plain ? c.take((size_t)J.total * 2 * al16((size_t)N * J.w)) : 0;
     J.o_aall = J.plain ? c.take((size_t)J.total * M * 4) : 0;
-    J.o_gslot = (!J.plain && J.pl.gslot) ? c.take((size_t)J.pl.grid * slot_bytes(J.m, J.gen)) : 0;
+    J.o_gslot = (!J.plain && J.pl.gslot) ? c.take((size_t)J.pl.grid * slot_bytes(J.m, J.mode != kModeFast)) : 0;
 }
 
 static tl_status job_bind(Job& J, unsigned char* B, cudaStream_t st) {
@@ -469,7 +469,7 @@ static tl_status job_bind(Job& J, unsigned char* B, cudaStream_t st) {
     p.off_vc = m->d.off_vc;
     p.off_cp = m->d.off_cp;
     p.off_rv = m->d.off_rv;
-    p.slot_bytes = (int)slot_bytes(m, J.gen);
+    p.slot_bytes = (int)slot_bytes(m, J.mode != kModeFast);
     p.row_warp = J.pl.row_warp ? 1 : 0;
     p.gslots = J.pl.gslot ? B + J.o_gslot : nullptr;
     p.ctr = rb.ctr;
@@ -610,7 +610,7 @@ static tl_status autotune_measure(Job& J, cudaStream_t st) {
         Cand win{0, 0, false};
         for (const Cand& c : cands) {
             Plan pl;
-            if (make_plan(m, c.variant, c.block, J.gen, J.compat_stoich, c.nostage, trial, pl) != TL_OK) continue;
+            if (make_plan(m, c.variant, c.block, J.mode, J.compat_stoich, c.nostage, trial, pl) != TL_OK) continue;
             if (c.variant == TL_VARIANT_THREAD && c.block != pl.block) continue;
             // global slots exist for the launch the heuristic planned
             if (pl.gslot && (!planned_gslot || pl.grid > planned_grid)) continue;
@@ -619,8 +619,8 @@ static tl_status autotune_measure(Job& J, cudaStream_t st) {
             tp.gslots = pl.gslot ? planned_gslots : nullptr;
             if (cudaMemsetAsync(tp.ctr, 0, 64, st) != cudaSuccess) break;
             cudaEventRecord(e0, st);
-            cudaError_t le = J.w == 8 ? launch_fused<long long>(tp, launch_kind(pl), J.gen, pl.block, pl.grid, pl.smem, st)
-                                      : launch_fused<int>(tp, launch_kind(pl), J.gen, pl.block, pl.grid, pl.smem, st);
+            cudaError_t le = J.w == 8 ? launch_fused<long long>(tp, launch_kind(pl), J.mode, pl.block, pl.grid, pl.smem, st)
+                                      : launch_fused<int>(tp, launch_kind(pl), J.mode, pl.block, pl.grid, pl.smem, st);
             cudaEventRecord(e1, st);
             if (le != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
                 cudaGetLastError();
@@ -645,13 +645,13 @@ static tl_status autotune_measure(Job& J, cudaStream_t st) {
         m->tuned_block = win.block;
         m->tuned_nostage = win.nostage ? 1 : 0;
     }
-    tl_status ps = make_plan(m, m->tuned_variant, m->tuned_block, J.gen, J.compat_stoich, m->tuned_nostage != 0,
+    tl_status ps = make_plan(m, m->tuned_variant, m->tuned_block, J.mode, J.compat_stoich, m->tuned_nostage != 0,
                              J.total, J.pl);
     if (ps != TL_OK) return ps;
     if (J.pl.gslot && (!planned_gslot || J.pl.grid > planned_grid)) {
         // a cached global-slot plan that needs more slots than were laid out:
         // keep the planned launch
-        ps = make_plan(m, TL_VARIANT_AUTO, 0, J.gen, J.compat_stoich, (J.cfg->flags & TL_FLAG_NO_STAGE) != 0,
+        ps = make_plan(m, TL_VARIANT_AUTO, 0, J.mode, J.compat_stoich, (J.cfg->flags & TL_FLAG_NO_STAGE) != 0,
                        J.total, J.pl);
         if (ps != TL_OK) return ps;
     }
@@ -675,7 +675,7 @@ static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad
     const bool no_stage = (cfg->flags & TL_FLAG_NO_STAGE) != 0;
     const bool measure = !J.plain && cfg->variant == TL_VARIANT_AUTO && (cfg->flags & TL_FLAG_AUTOTUNE_MEASURE);
     if (!J.plain) {
-        ps = make_plan(m, cfg->variant, cfg->block_threads, J.gen, J.compat_stoich, no_stage, J.total, J.pl);
+        ps = make_plan(m, cfg->variant, cfg->block_threads, J.mode, J.compat_stoich, no_stage, J.total, J.pl);
         if (ps != TL_OK) return ps;
     } else {
         J.pl.variant = TL_VARIANT_PLAIN;
@@ -704,8 +704,8 @@ static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad
     cudaError_t le = cudaEventRecord(e0, st);
     if (le == cudaSuccess) {
         if (!J.plain) {
-            le = w == 8 ? launch_fused<long long>(p, launch_kind(J.pl), J.gen, J.pl.block, J.pl.grid, J.pl.smem, st)
-                        : launch_fused<int>(p, launch_kind(J.pl), J.gen, J.pl.block, J.pl.grid, J.pl.smem, st);
+            le = w == 8 ? launch_fused<long long>(p, launch_kind(J.pl), J.mode, J.pl.block, J.pl.grid, J.pl.smem, st)
+                        : launch_fused<int>(p, launch_kind(J.pl), J.mode, J.pl.block, J.pl.grid, J.pl.smem, st);
             launches = 1;
         } else {
             le = w == 8 ? launch_plain_init<long long>(p, st) : launch_plain_init<int>(p, st);
@@ -821,7 +821,7 @@ static tl_status run_batch(tl_batch_item* items, int n, cudaStream_t st) {
     for (int i = 0; i < n; ++i) {
         const tl_model* m = jobs[(size_t)i].m;
         lane[(size_t)i] = (m->h.M <= 16 && m->h.N <= 16) ? 1 : 0;
-        const size_t sbi = slot_bytes(m, jobs[(size_t)i].gen);
+        const size_t sbi = slot_bytes(m, jobs[(size_t)i].mode != kModeFast);
         const size_t need = lane[(size_t)i] ? 32 * sbi : sbi;
         wslot = std::max(wslot, need);
         Plan& pl = jobs[(size_t)i].pl;
@@ -904,12 +904,12 @@ static tl_status run_batch(tl_batch_item* items, int n, cudaStream_t st) {
     bp.warp_slot_bytes = (int)wslot;
     bp.params_bytes = (int)spb;
     bp.wctr = reinterpret_cast<unsigned long long*>(B + o_wctr);
-    bool any_sens = false;  // the general kernel: scores or compatibility switches in any item
-    for (auto& J : jobs) any_sens |= J.gen;
+    int bmode = kModeFast;  // the build every item can run on
+    for (auto& J : jobs) bmode = std::max(bmode, J.mode);
     const size_t smem = stage + (size_t)warps * (wslot + spb);
     int bps = 0;
-    cudaError_t le = pop == 64 ? batch_occupancy<long long>(any_sens, 32 * warps, smem, &bps)
-                               : batch_occupancy<int>(any_sens, 32 * warps, smem, &bps);
+    cudaError_t le = pop == 64 ? batch_occupancy<long long>(bmode, 32 * warps, smem, &bps)
+                               : batch_occupancy<int>(bmode, 32 * warps, smem, &bps);
     if (le != cudaSuccess) return cuda_fail(le, "batch occupancy");
     const int grid = (int)std::min<long long>((long long)sm_count() * std::max(bps, 1),
                                               (units + warps - 1) / warps);
@@ -919,8 +919,8 @@ static tl_status run_batch(tl_batch_item* items, int n, cudaStream_t st) {
     TLC(cudaEventCreate(&e1));
     le = cudaEventRecord(e0, st);
     if (le == cudaSuccess)
-        le = pop == 64 ? launch_batch<long long>(bp, any_sens, 32 * warps, grid, smem, st)
-                       : launch_batch<int>(bp, any_sens, 32 * warps, grid, smem, st);
+        le = pop == 64 ? launch_batch<long long>(bp, bmode, 32 * warps, grid, smem, st)
+                       : launch_batch<int>(bp, bmode, 32 * warps, grid, smem, st);
     if (le == cudaSuccess) le = cudaEventRecord(e1, st);
     if (le != cudaSuccess) {
         cudaEventDestroy(e0);
@@ -1438,7 +1438,7 @@ extern "C" tl_status tl_simulate_static(tl_model* m, const tl_run_cfg* cfg, tl_r
     if (ps != TL_OK) return ps;
     TLC(cudaSetDevice(m->d.device));
     cudaStream_t st = (cudaStream_t)cfg->stream;
-    ps = make_plan(m, cfg->variant, cfg->block_threads, J.gen, J.compat_stoich,
+    ps = make_plan(m, cfg->variant, cfg->block_threads, J.mode, J.compat_stoich,
                    (cfg->flags & TL_FLAG_NO_STAGE) != 0, J.total, J.pl);
     if (ps != TL_OK) return ps;
     Carver c;
@@ -1455,8 +1455,8 @@ extern "C" tl_status tl_simulate_static(tl_model* m, const tl_run_cfg* cfg, tl_r
     ps = job_bind(J, reinterpret_cast<unsigned char*>(base), st);  // clears the counters
     if (ps != TL_OK) return ps;
     const auto tk = std::chrono::steady_clock::now();
-    cudaError_t le = J.w == 8 ? launch_fused<long long>(J.p, launch_kind(J.pl), J.gen, J.pl.block, J.pl.grid, J.pl.smem, st)
-                              : launch_fused<int>(J.p, launch_kind(J.pl), J.gen, J.pl.block, J.pl.grid, J.pl.smem, st);
+    cudaError_t le = J.w == 8 ? launch_fused<long long>(J.p, launch_kind(J.pl), J.mode, J.pl.block, J.pl.grid, J.pl.smem, st)
+                              : launch_fused<int>(J.p, launch_kind(J.pl), J.mode, J.pl.block, J.pl.grid, J.pl.smem, st);
     if (le != cudaSuccess) return cuda_fail(le, "simulation launch");
     ps = job_reduce(J, st);
     if (ps != TL_OK) return ps;

@@ -195,13 +195,14 @@ TL_D void run_realization(const Grp& g, const SimParams& p, const MView& mv, Slo
 #ifndef TL_BATCH_MINB
 #define TL_BATCH_MINB 2
 #endif
-// GEN: the general kernel, with the likelihood-ratio scores and the
-// reference-compatibility switches; the other build has neither (about 6 %
-// faster: smaller code, fewer registers spilled).
+// MODE: kModeFast has neither likelihood-ratio scores nor the
+// reference-compatibility switches; kModeScores has the scores;
+// kModeGeneral has both.  Smaller builds spill fewer registers: the fast
+// one is ~6 % faster than the general one, and the scores-only batch 15 %.
 // GSLOT (CTA groups only): each CTA's slot lives in global memory, for
 // realizations whose state exceeds shared memory.  A separate build, so
 // that the shared-memory kernels keep shared-memory addressing.
-template <int KIND, class Pop, bool GEN, bool GSLOT = false>
+template <int KIND, class Pop, int MODE, bool GSLOT = false>
 __global__ void __launch_bounds__(KIND == 0 ? 1024 : 256, KIND == 0 ? 1 : KIND == 1 ? TL_THREAD_MINB : TL_WARP_MINB)
     k_fused(SimParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -230,7 +231,7 @@ __global__ void __launch_bounds__(KIND == 0 ? 1024 : 256, KIND == 0 ? 1 : KIND =
         if (g.leader()) w = (long long)atomicAdd(p.ctr + 0, 1ull);
         w = g.bcast(w, 0);
         if (w >= total) break;
-        run_realization<Grp, Pop, GEN, GEN>(g, p, mv, s, w, nl, ns, nr, ntr);
+        run_realization<Grp, Pop, (MODE >= kModeScores), (MODE == kModeGeneral)>(g, p, mv, s, w, nl, ns, nr, ntr);
     }
     if (g.leader()) {
         if (nl) atomicAdd(p.ctr + 1, (unsigned long long)nl);
@@ -250,7 +251,7 @@ TL_D void add_counts(unsigned long long* ctr, long long nl, long long ns, long l
     if (ntr) atomicAdd(ctr + 4, (unsigned long long)ntr);
 }
 
-template <class Pop, bool GEN>
+template <class Pop, int MODE>
 __global__ void __launch_bounds__(256, TL_BATCH_MINB) k_batch(BatchParams bp) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ __align__(8) unsigned long long mbar;
@@ -291,14 +292,16 @@ __global__ void __launch_bounds__(256, TL_BATCH_MINB) k_batch(BatchParams bp) {
         if (!bp.items[it].lane_mode) {
             const GWarp g{lane};
             Slot<Pop> s = carve_slot<Pop>(wslot, p);
-            run_realization<GWarp, Pop, GEN, GEN>(g, p, mv, s, local, a, b, c, d);
+            run_realization<GWarp, Pop, (MODE >= kModeScores), (MODE == kModeGeneral)>(g, p, mv, s, local, a, b,
+                                                                                      c, d);
             if (lane == 0) add_counts(p.ctr, a, b, c, d);  // state is replicated across the warp
         } else {
             const long long wi = local * 32 + lane;
             if (wi < p.R * (long long)p.S) {
                 const G1 g{};
                 Slot<Pop> s = carve_slot<Pop>(wslot + (size_t)lane * p.slot_bytes, p);
-                run_realization<G1, Pop, GEN, GEN>(g, p, mv, s, wi, a, b, c, d);
+                run_realization<G1, Pop, (MODE >= kModeScores), (MODE == kModeGeneral)>(g, p, mv, s, wi, a, b, c,
+                                                                                     d);
                 add_counts(p.ctr, a, b, c, d);
             }
         }

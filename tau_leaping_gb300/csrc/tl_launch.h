@@ -11,22 +11,26 @@ struct SimParams;
 // kind: 1 = thread, 32 = warp, 0 = CTA, 2/4/8/16 = lanes per realization,
 // kKindCtaGlobal = CTA with its slot in global memory.
 constexpr int kKindCtaGlobal = 64;
+// mode: the kernel build a run needs.  Fast: no likelihood-ratio scores and
+// no reference-compatibility switches; Scores: with scores; General: both.
+// The sub-warp and global-slot kinds come in Fast and General only.
+constexpr int kModeFast = 0, kModeScores = 1, kModeGeneral = 2;
 template <class Pop>
-cudaError_t launch_fused(const SimParams& p, int kind, bool gen, int block, int grid, size_t smem,
+cudaError_t launch_fused(const SimParams& p, int kind, int mode, int block, int grid, size_t smem,
                          cudaStream_t st);
 template <class Pop>
-cudaError_t fused_occupancy(int kind, bool gen, int block, size_t smem, int* blocks_per_sm);
+cudaError_t fused_occupancy(int kind, int mode, int block, size_t smem, int* blocks_per_sm);
 // sub-warp kinds (2, 4, 8, 16 lanes per realization), compiled in their own units
 template <class Pop>
-cudaError_t launch_fused_sub(const SimParams& p, int kind, bool gen, int block, int grid, size_t smem,
+cudaError_t launch_fused_sub(const SimParams& p, int kind, int mode, int block, int grid, size_t smem,
                              cudaStream_t st);
 template <class Pop>
-cudaError_t fused_occupancy_sub(int kind, bool gen, int block, size_t smem, int* blocks_per_sm);
+cudaError_t fused_occupancy_sub(int kind, int mode, int block, size_t smem, int* blocks_per_sm);
 struct BatchParams;
 template <class Pop>
-cudaError_t launch_batch(const BatchParams& bp, bool gen, int block, int grid, size_t smem, cudaStream_t st);
+cudaError_t launch_batch(const BatchParams& bp, int mode, int block, int grid, size_t smem, cudaStream_t st);
 template <class Pop>
-cudaError_t batch_occupancy(bool gen, int block, size_t smem, int* blocks_per_sm);
+cudaError_t batch_occupancy(int mode, int block, size_t smem, int* blocks_per_sm);
 template <class Pop>
 cudaError_t launch_plain_init(const SimParams& p, cudaStream_t st);
 template <class Pop>
