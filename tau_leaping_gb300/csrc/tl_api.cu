@@ -190,8 +190,9 @@ static int launch_kind(const Plan& pl) { return pl.gslot ? kKindCtaGlobal : pl.k
 //    every SM gets work;
 //  * per-realization state up to 8 KB: one warp per realization, 256-thread
 //    blocks, model tables staged in shared memory;
-//  * up to 64 KB: one 256-thread CTA per realization, tables through L1/L2
-//    (chain-sized models: 1024 species and channels);
+//  * up to 64 KB: one 128-thread (up to 1024 channels) or 256-thread CTA per
+//    realization, tables through L1/L2 (chain-sized models: 1024 species
+//    and channels);
 //  * larger: one 1024-thread CTA per realization (propensities of ~30k
 //    channels fill most of the 227 KB of shared memory).
 // The choices follow a sweep of every (variant, block, staging) plan on the
@@ -232,7 +233,10 @@ static tl_status make_plan(const tl_model* m, int variant, int block_req, int mo
         groups_per_block = pl.block / pl.kind;
     } else if (variant == TL_VARIANT_CTA) {
         pl.kind = 0;
-        pl.block = block_req > 0 ? block_req : (sb <= 64 * 1024 ? 256 : 1024);
+        // chain-sized models (up to 1024 channels): 128 threads, 8 channels
+        // each (cyclic chain 1024: 3.67e7 realization-steps/s against 3.41e7
+        // at 256); up to 64 KB of state: 256; larger: 1024
+        pl.block = block_req > 0 ? block_req : (sb <= 64 * 1024 ? (m->h.M <= 1024 ? 128 : 256) : 1024);
         groups_per_block = 1;
     } else {
         set_last_error("unknown variant");
