@@ -5,7 +5,7 @@
 //   tl_cli -f model.xml -t T -n R -r S1 S5 [-e eps] [-i intervals]
 //          [-a max_steps] [-b name] [-d device]
 //          [--seed S] [--compat] [--variant auto|thread|lanes2|lanes4|lanes8|lanes16|warp|cta|plain]
-//          [--pop64] [--samples file]
+//          [--autotune] [--pop64] [--samples file]
 //
 // Writes mean_<name>.txt and stddev_<name>.txt, one line per grid time
 // "t v1 v2 ..." for the tracked species in species order, like StatToFile
@@ -42,6 +42,7 @@ struct Args {
     int device = 0;
     unsigned long long seed = 1;
     bool compat = false;
+    bool autotune = false;
     int variant = TL_VARIANT_AUTO;
     int pop_bits = 0;
     std::string samples_file;
@@ -50,8 +51,8 @@ struct Args {
 void usage() {
     std::cerr << "usage: tl_cli -f <model.xml> -t <t_final> -n <realizations> -r <species ...|all>\n"
                  "              [-e eps] [-i intervals] [-a max_steps] [-b name] [-d device]\n"
-                 "              [--seed S] [--compat] [--variant auto|thread|lanes2|lanes4|lanes8|lanes16|warp|cta|plain] [--pop64]\n"
-                 "              [--samples file]\n";
+                 "              [--seed S] [--compat] [--variant auto|thread|lanes2|lanes4|lanes8|lanes16|warp|cta|plain]\n"
+                 "              [--autotune] [--pop64] [--samples file]\n";
 }
 
 bool parse(int argc, char** argv, Args& a) {
@@ -104,6 +105,8 @@ bool parse(int argc, char** argv, Args& a) {
             a.seed = strtoull(v, nullptr, 10);
         } else if (k == "--compat") {
             a.compat = true;
+        } else if (k == "--autotune") {
+            a.autotune = true;
         } else if (k == "--pop64") {
             a.pop_bits = 64;
         } else if (k == "--samples") {
@@ -182,6 +185,7 @@ int main(int argc, char** argv) {
     cfg.variant = a.variant;
     cfg.max_steps = a.max_steps;
     if (a.compat) cfg.flags |= TL_FLAG_COMPAT_REFERENCE;
+    if (a.autotune) cfg.flags |= TL_FLAG_AUTOTUNE_MEASURE;
     const size_t P = (size_t)a.intervals + 1, K = tracked.size();
     std::vector<double> times(P), mean(P * K), sd(P * K);
     std::vector<int64_t> samples;
