@@ -132,6 +132,22 @@ def test_edge_cases():
         assert e.value.status == 1
 
 
+@pytest.mark.parametrize("variant", [_ffi.VARIANT_THREAD, _ffi.VARIANT_LANES4, _ffi.VARIANT_LANES16,
+                                     _ffi.VARIANT_WARP, _ffi.VARIANT_CTA])
+def test_int64_populations_on_every_group_kind(variant):
+    """The dimer with 64-bit populations through each group kind: the same
+    ensemble statistics as the FP64 oracle, and the same trajectories as the
+    32-bit build of the model (its populations stay far below 2^31)."""
+    d = dimer(2000).desc()
+    m32 = Model.from_arrays(d["x0"], d["rate"], d["col_ptr"], d["row_ind"], d["stoich"], pop_bits=32)
+    m64 = Model.from_arrays(d["x0"], d["rate"], d["col_ptr"], d["row_ind"], d["stoich"], pop_bits=64)
+    kw = dict(t_final=1.0, n=2048, seed=7, tracked=[0, 1], keep_samples=True, variant=variant)
+    a, b = m64.simulate(**kw), m32.simulate(**kw)
+    assert np.array_equal(a.samples, b.samples)
+    r = ora.OracleModel.from_desc(d).simulate(1.0, 2048, seed=8, tracked=[0, 1], threads=8)
+    compare_final(a.samples[0, :, -1, :], r["samples"][0, :, -1, :], f"int64 variant {variant}")
+
+
 def test_int32_overflow_detected():
     # S1 -> 2 S1 from 2^30: grows past int32 within t=2
     m = Model.from_arrays([2**30], [1.0], [0, 2], [0, 0], [-1, 2], pop_bits=32)
