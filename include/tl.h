@@ -167,6 +167,11 @@ enum tl_variant {
 #define TL_FLAG_NO_STAGE (1u << 3)       /* read model tables through L1/L2
                                             instead of staging them in
                                             shared memory (tuning knob)     */
+#define TL_FLAG_GLOBAL_SLOTS (1u << 5)  /* CTA groups: keep each realization's
+                                            state in global memory (L2) even
+                                            when it fits in shared memory
+                                            (tuning and checking knob; larger
+                                            states always do)              */
 #define TL_FLAG_GRAPH (1u << 4)          /* PLAIN: replay the per-step launches
                                             as a captured CUDA graph of 16
                                             steps between completion polls  */

@@ -30,6 +30,7 @@ FLAG_KEEP_SAMPLES = 1 << 1
 FLAG_AUTOTUNE_MEASURE = 1 << 2
 FLAG_NO_STAGE = 1 << 3
 FLAG_GRAPH = 1 << 4
+FLAG_GLOBAL_SLOTS = 1 << 5
 FLAG_COMPAT_G = 1 << 8
 FLAG_COMPAT_CRIT = 1 << 9
 FLAG_COMPAT_STOICH = 1 << 10

@@ -204,7 +204,7 @@ static int heuristic_variant(const tl_model* m, size_t sb) {
 }
 
 static tl_status make_plan(const tl_model* m, int variant, int block_req, int mode, bool compat_stoich,
-                           bool no_stage, long long total, Plan& pl) {
+                           bool no_stage, long long total, Plan& pl, bool force_gslot = false) {
     const size_t sb = slot_bytes(m, mode != kModeFast);
     const int smax = max_smem_optin() - 2048;
     const int stage = (compat_stoich || no_stage) ? 0 : m->d.stage_bytes;
@@ -252,6 +252,7 @@ static tl_status make_plan(const tl_model* m, int variant, int block_req, int mo
         pl.block -= 32;
         groups_per_block = pl.block / pl.kind;
     }
+    if (force_gslot && pl.kind == 0) pl.gslot = true;
     if ((size_t)groups_per_block * sb > (size_t)smax) {
         if (pl.kind != 0) {
             set_last_error("model too large for the shared-memory slot of this variant");
@@ -679,7 +680,8 @@ static tl_status run(tl_model* m, const tl_run_cfg* cfg, tl_result* res, tl_grad
     const bool no_stage = (cfg->flags & TL_FLAG_NO_STAGE) != 0;
     const bool measure = !J.plain && cfg->variant == TL_VARIANT_AUTO && (cfg->flags & TL_FLAG_AUTOTUNE_MEASURE);
     if (!J.plain) {
-        ps = make_plan(m, cfg->variant, cfg->block_threads, J.mode, J.compat_stoich, no_stage, J.total, J.pl);
+        ps = make_plan(m, cfg->variant, cfg->block_threads, J.mode, J.compat_stoich, no_stage, J.total, J.pl,
+                       (cfg->flags & TL_FLAG_GLOBAL_SLOTS) != 0);
         if (ps != TL_OK) return ps;
     } else {
         J.pl.variant = TL_VARIANT_PLAIN;

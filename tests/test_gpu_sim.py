@@ -229,6 +229,18 @@ def test_state_larger_than_shared_memory_runs_from_global_slots():
     assert np.array_equal(g.samples, h.samples)
 
 
+def test_global_slots_are_bit_identical_to_shared_slots():
+    """TL_FLAG_GLOBAL_SLOTS moves a CTA group's state to global memory; the
+    arithmetic is the same, so the trajectories are too."""
+    m = Model.generate("colloid", n_species=60)
+    kw = dict(t_final=0.005, n=512, seed=3, tracked=[0, 1, 9], keep_samples=True, intervals=2,
+              variant=_ffi.VARIANT_CTA)
+    a = m.simulate(**kw)
+    b = m.simulate(flags=_ffi.FLAG_GLOBAL_SLOTS, **kw)
+    assert np.array_equal(a.samples, b.samples)
+    assert (a.leaps, a.ssa_steps, a.rejections) == (b.leaps, b.ssa_steps, b.rejections)
+
+
 def test_measured_autotuner_picks_a_plan_and_caches_it():
     m = Model.generate("toy", n_species=32, n_channels=64, seed=4, x0_max=3000)
     o = ora.OracleModel.from_desc(m.desc())
