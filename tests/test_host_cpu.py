@@ -30,6 +30,35 @@ def test_library_exports_every_declared_symbol():
         assert lib.tl_status_str(s)
 
 
+def test_integration_binding_compiles_and_links(tmp_path):
+    """The C++ `Model` class that INTEGRATION.md gives a maintainer of the
+    reference builds against include/tl.h and links against libtl.so."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    text = (ROOT / "INTEGRATION.md").read_text()
+    code = re.search(r"```cpp\n(.*?)```", text, flags=re.S).group(1)
+    (tmp_path / "gpu_model.h").write_text(code)
+    (tmp_path / "main.cpp").write_text(
+        '#include "gpu_model.h"\n'
+        "int main(int argc, char** argv) {\n"
+        "    if (argc < 2) return 0;\n"
+        "    std::vector<std::string> names;\n"
+        "    Model* m = Model::ReadXML(argv[1], names);\n"
+        "    std::vector<char> track(m->ReactantsCount(), 1);\n"
+        "    std::vector<double> mean, sd, t;\n"
+        "    m->PerformCalcAll(0.1f, 0.03f, track, 100, 2, 0x7fffffff, 1, mean, sd, t);\n"
+        "    delete m;\n"
+        "}\n")
+    lib = ROOT / "tau_leaping_gb300"
+    r = subprocess.run([gxx, "-std=c++17", "-I", str(ROOT / "include"), str(tmp_path / "main.cpp"), "-L", str(lib),
+                        "-ltl", f"-Wl,-rpath,{lib}", "-o", str(tmp_path / "a.out")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert subprocess.run([str(tmp_path / "a.out")]).returncode == 0  # no model given: exits before any GPU call
+
+
 def dimer_arrays(s1=100000):
     # channel-major entries exactly as ReadXMLToMatrixStruct would list them
     col_ptr = [0, 1, 3, 5, 7]
