@@ -15,7 +15,8 @@ separately, with seconds per 1e4 realizations to t_final.
 
 --impl reference times the CPU path (the FP64 oracle port of the
 reference's algorithm, all host threads) on a bounded sample of the same
-workload and prints the same line with "impl": "reference".
+workload and prints the same line with "impl": "reference".  That arm builds
+its model with the oracle's own generator and never loads the engine.
 
 Multi-GPU (torchrun): realizations are sharded by realization id, each rank
 runs its own R (weak scaling), no collective on the data path; rank 0 prints
@@ -25,6 +26,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes as C
+import hashlib
 import json
 import os
 import statistics
@@ -42,22 +44,39 @@ METRIC = "realization-leaps/sec"
 UNIT = "realization-steps/s"
 
 WORKLOADS = {
-    # name: generator family, t_final, realizations, tracked species, pop bits
-    "toy": dict(family="toy", t_final=0.1, R=100_000, tracked=[0, 4],
+    # name: generator family, t_final, realizations, tracked species, sizes
+    "toy": dict(family="toy", t_final=0.1, R=100_000, tracked=[0, 4], n_species=128, n_channels=256, pop_bits=32,
                 desc="random toy network 128 species x 256 channels (seed 7), t_final 0.1, 1e5 realizations, "
                      "track S1,S5"),
-    "dimer": dict(family="dimer", t_final=10.0, R=10_000, tracked=[0, 1],
+    "dimer": dict(family="dimer", t_final=10.0, R=10_000, tracked=[0, 1], n_species=3, n_channels=4, pop_bits=32,
                   desc="dimerisation decay S1=1e5, t_final 10, 1e4 realizations, track S1,S2"),
-    "chain": dict(family="chain", t_final=1.0, R=65_536, tracked=[0, 1],
-                  desc="cyclic chain 1024 species (seed 11), t_final 1, 65536 realizations"),
-    "colloid": dict(family="colloid", t_final=0.01, R=4096, tracked=[0, 1],
-                    desc="colloidal aggregation 250 species x 31250 channels (seed 13), t_final 0.01, "
-                         "4096 realizations, int64"),
-    "batch": dict(family="batch", t_final=None, R=None, tracked=[0, 1],
+    "chain": dict(family="chain", t_final=1.0, R=65_536, tracked=[0, 1], n_species=1024, n_channels=1024,
+                  pop_bits=32, desc="cyclic chain 1024 species (seed 11), t_final 1, 65536 realizations"),
+    "colloid": dict(family="colloid", t_final=0.01, R=4096, tracked=[0, 1], n_species=250, n_channels=31250,
+                    pop_bits=64, desc="colloidal aggregation 250 species x 31250 channels (seed 13), t_final 0.01, "
+                                      "4096 realizations, int64"),
+    "batch": dict(family="batch", t_final=None, R=None, tracked=[0, 1], n_species=None, n_channels=None, pop_bits=32,
                   desc="one launch: dimer-decay 64 rate sets (c x lognormal(0,0.2), seed 17) x 4096 realizations, "
                        "t_final U[1,10]; toy network 16 rate sets x 1024 realizations, t_final U[0.05,0.1]; "
                        "likelihood-ratio sensitivities on"),
 }
+
+# Element operations of one realization-step (the issue-roof figure): per
+# channel a propensity and a Poisson draw, per stored entry the mu and
+# sigma^2 FMAs and the integer update.
+def ops_per_step(N: int, M: int, nnz: int) -> int:
+    return 2 * M + 3 * nnz
+
+
+def dtype_of(wl) -> str:
+    return "fp32+int64" if wl["pop_bits"] == 64 else "fp32+int32"
+
+
+def workload_config(wl, R, T, world) -> dict:
+    """The config both arms report (identical for the same workload)."""
+    return {"workload": wl["desc"], "realizations_per_gpu": R, "t_final": T, "n_species": wl["n_species"],
+            "n_channels": wl["n_channels"], "population": "int64" if wl["pop_bits"] == 64 else "int32",
+            "parallelism": f"realizations sharded over {world} process(es)"}
 
 
 def batch_items(seed=1, scale=1.0):
@@ -147,17 +166,31 @@ def model_bytes(m) -> tuple[int, int]:
     return blob + N * w + 4 * M, w
 
 
-def profile_traffic(workload: str):
-    """DRAM bytes (read + write) per launch of the fused kernel on this
-    workload, from the committed ncu summary (profiles/), or None."""
-    p = ROOT / "profiles" / f"k_fused_{workload}.md"
+def kernel_source_hash() -> str:
+    """sha256 of everything that determines the fused kernel's machine code:
+    the CUDA sources, the C ABI header and the nvcc flags."""
+    from tau_leaping_gb300 import build as b
+    h = hashlib.sha256()
+    for p in sorted(b.CSRC.glob("*")) + sorted(b.INC.glob("*.h")):
+        h.update(p.name.encode())
+        h.update(p.read_bytes())
+    h.update(" ".join(b.NVFLAGS).encode())
+    return h.hexdigest()
+
+
+def ncu_record(kernel_tag: str):
+    """The ncu figures of the fused kernel on this workload (DRAM bytes per
+    launch, issue-slot utilisation), from the record kept beside the
+    profile summaries, used only if it was captured from this very kernel
+    build (same source hash); otherwise None and the reason."""
+    p = ROOT / "profiles" / f"{kernel_tag}.ncu.json"
     try:
-        for line in p.read_text().splitlines():
-            if line.startswith("dram_bytes_per_launch:"):
-                return int(float(line.split(":", 1)[1]))
-    except OSError:
-        pass
-    return None
+        rec = json.loads(p.read_text())
+    except (OSError, ValueError):
+        return None, "no ncu record for this workload"
+    if rec.get("source_sha256") != kernel_source_hash():
+        return None, "ncu record is from another kernel build"
+    return rec, "ncu capture of this kernel build"
 
 
 def alg_bytes_per_step(m) -> int:
@@ -199,9 +232,10 @@ def run_batch_workload(args, wl, rank, world, local_rank):
     o = outs[-1]
     line = {"metric": METRIC, "value": steps / (tot / 1e3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tot / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "fp32+int32", "data": "synthetic (seeded generator)",
-            "config": {"workload": wl["desc"], "variant": "batched (lane units + warp units)",
-                       "grid": o[0]["grid"], "block_threads": o[0]["block_threads"]},
+            "vs_baseline": None, "dtype": dtype_of(wl), "data": "synthetic (seeded generator)",
+            "config": {"workload": wl["desc"], "parallelism": f"realizations sharded over {world} process(es)"},
+            "launch": {"variant": "batched (lane units + warp units)", "grid": o[0]["grid"],
+                       "block_threads": o[0]["block_threads"]},
             "leaps_per_step": float(sum(it["leaps"] for it in o)),
             "ssa_steps_per_step": float(sum(it["ssa_steps"] for it in o)),
             "gpu_launches": args.steps * (1 + 2 * len(items)),
@@ -214,7 +248,6 @@ def run_ours(args, wl, rank, world, local_rank):
     import torch
 
     from tau_leaping_gb300 import Model, _ffi
-    from tau_leaping_gb300.model import _ptr
 
     if wl["family"] == "batch":
         return run_batch_workload(args, wl, rank, world, local_rank)
@@ -272,42 +305,56 @@ def run_ours(args, wl, rank, world, local_rank):
     k_ms = float(np.mean(kms))
     steps_per_launch = float(np.mean(steps))
     alg_per_launch = alg_bytes_per_step(m) * steps_per_launch
+    stream_gbs = alg_per_launch / (k_ms / 1e3) / 1e9
     # bytes that must cross HBM per launch: constants once, samples out
     cbytes, w = model_bytes(m)
     hbm_alg = cbytes + R * (1 + 1) * len(tracked) * w
     pk = peaks()
+    ops = ops_per_step(m.n_species, m.n_channels, m.nnz_net)
+    rec, rec_src = ncu_record(f"k_fused_{args.workload}") if args.variant == 0 and not args.t_final and \
+        not args.realizations else (None, "ncu record covers the default launch only")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "fp32+int32", "data": "synthetic (seeded generator)",
-        "config": {"workload": wl["desc"], "realizations_per_gpu": R, "t_final": T,
-                   "n_species": m.n_species, "n_channels": m.n_channels, "variant": r0.variant,
-                   "grid": r0.grid, "block_threads": r0.block_threads, "l2": "flushed between steps (256 MB write)",
-                   "parallelism": f"realizations sharded over {world} GPU(s)"},
+        "scaling": "weak", "vs_baseline": None, "dtype": dtype_of(wl), "data": "synthetic (seeded generator)",
+        "config": workload_config(wl, R, T, world),
+        "timing": "CUDA events on the library's stream around each tl_simulate call; L2 flushed between steps "
+                  "(256 MB write)",
+        "launch": {"variant": r0.variant, "grid": r0.grid, "block_threads": r0.block_threads},
         "leaps_per_step": float(np.mean([r.leaps for r in results])),
         "ssa_steps_per_step": float(np.mean([r.ssa_steps for r in results])),
         "rejections_per_step": float(np.mean([r.rejections for r in results])),
         "sec_per_1e4_realizations": (tot_ms / args.steps / 1e3) * 1e4 / R,
         "gpu_launches": args.steps * (r0.launches + 1),
-        "roofline": {"bound": "hbm", "achieved": alg_per_launch / (k_ms / 1e3) / 1e9, "peak": pk["hbm_gbs"],
-                     "unit": "GB/s", "frac": alg_per_launch / (k_ms / 1e3) / 1e9 / pk["hbm_gbs"],
-                     "traffic": profile_traffic(args.workload), "peak_src": pk["src"], "kernel": "k_fused",
-                     "kernel_ms": k_ms, "alg_bytes_per_step": alg_bytes_per_step(m),
-                     "steps_per_launch": steps_per_launch,
-                     "hbm_required_gbs": hbm_alg / (k_ms / 1e3) / 1e9,
-                     "note": "achieved = algorithmic bytes per realization-step (model tables + populations "
-                             "read/written per leap) x steps per launch / launch time; the fused kernel serves "
-                             "them from shared memory, so DRAM traffic (ncu) is only the tables once per CTA "
-                             "plus the grid samples; the kernel is bound by instruction issue"},
+        "roofline": {
+            "bound": "issue", "achieved": stream_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": stream_gbs / pk["hbm_gbs"],
+            "traffic": rec["dram_bytes_per_launch"] if rec else None,
+            "issue_slots_busy": rec["issue_slots_busy_pct"] / 100.0 if rec else None,
+            "ncu_source": rec_src, "ncu_case": rec.get("case") if rec else None,
+            "peak_src": pk["src"], "kernel": "k_fused", "kernel_ms": k_ms,
+            "alg_bytes_per_step": alg_bytes_per_step(m), "steps_per_launch": steps_per_launch,
+            "ops_per_step": ops, "ops_per_s": ops * steps_per_launch / (k_ms / 1e3),
+            "hbm_required_gbs": hbm_alg / (k_ms / 1e3) / 1e9,
+            "note": "the fused kernel is bound by instruction issue (issue_slots_busy, from ncu on this kernel "
+                    "build); achieved is the algorithmic stream of a realization-step (model tables + populations "
+                    "read and written, B_alg) x steps per launch / launch time, served from shared memory and L1, "
+                    "against the HBM copy peak as a yardstick; DRAM carries only the tables once per CTA, the grid "
+                    "samples and local-memory lines (traffic)"},
     }
     # end to end through the C ABI with host buffers
     if rank == 0:
-        line["e2e"] = e2e(args, wl, m, R, T, stream, sptr)
+        line["e2e"] = e2e(args, wl, m, R, T, sptr)
         line["clocks"] = clk.summary()
         if world == 1 and not args.no_plain:
             line["plain_form"] = plain_form(args, wl, m, R, T, tot_ms / args.steps, sptr)
+            if args.workload != "colloid":
+                line["workloads"] = {"colloid": colloid_target(args, sptr)}
         if world == 1 and not args.no_cpu:
-            line["cpu_baseline"] = cpu_baseline(args, wl, m, R, check_gpu=True)
+            from oracle import py as ora
+            o = ora.OracleModel.from_desc(m.desc())
+            line["cpu_baseline"] = cpu_baseline(o, wl, R, T, args.seed)
+            line["cpu_baseline"]["fp64_check"] = fp64_check(args, wl, m, line["cpu_baseline"].pop("_finals"))
         print(json.dumps(line), flush=True)
 
 
@@ -334,9 +381,35 @@ def plain_form(args, wl, m, R, T, fused_ms, sptr, budget_s: float = 8.0):
             "note": "host wall time of each tl_simulate call (kernels + statistics), same sample"}
 
 
-def e2e(args, wl, m, R, T, stream, sptr):
+def colloid_target(args, sptr, reps: int = 2):
+    """The 250-species colloidal aggregation configuration in full (31250
+    channels, int64, 4096 realizations to t_final 0.01): the fused
+    persistent kernel against the plain form (one realization per thread,
+    one launch per step; the faster of its per-launch and graph-replayed
+    loops), each the mean of `reps` calls after one warm-up, timed by the
+    host around the whole call (kernels + statistics)."""
+    from tau_leaping_gb300 import Model, _ffi
+    m = Model.generate("colloid")
+    kw = dict(t_final=0.01, n=4096, seed=args.seed, tracked=[0, 1], stream=sptr)
+    out = {}
+    for name, var, fl in (("fused", 0, 0), ("plain", _ffi.VARIANT_PLAIN, 0),
+                          ("plain_graph", _ffi.VARIANT_PLAIN, _ffi.FLAG_GRAPH)):
+        m.simulate(**kw, variant=var, flags=fl)
+        rs = [m.simulate(**kw, variant=var, flags=fl) for _ in range(reps)]
+        st = sum(r.leaps + r.ssa_steps for r in rs)
+        ms = sum(r.total_ms for r in rs)
+        out[name] = {"value": st / (ms / 1e3), "ms_per_call": ms / reps, "launches": rs[-1].launches,
+                     "variant": rs[-1].variant}
+    plain = max(out["plain"]["value"], out["plain_graph"]["value"])
+    return {"workload": WORKLOADS["colloid"]["desc"], "unit": UNIT, "fused": out["fused"],
+            "plain": out["plain"], "plain_graph": out["plain_graph"], "speedup_vs_plain": out["fused"]["value"] / plain,
+            "target": ">= 5x the plain form (FP32, one realization per thread, one launch per step)"}
+
+
+def e2e(args, wl, m, R, T, sptr, n: int = 3):
     """Same metric through tl_model_create + tl_simulate from host arrays:
-    every step uploads the model, runs, and reads the statistics back."""
+    every sample uploads the model, runs, and reads the statistics back;
+    the mean over n samples."""
     import torch
 
     from tau_leaping_gb300 import Model
@@ -344,9 +417,8 @@ def e2e(args, wl, m, R, T, stream, sptr):
     tr = wl["tracked"]
     h2d = model_bytes(m)[0] + 8 * len(tr) + 8
     d2h = 2 * 2 * len(tr) * 8 + 64
-    tot, steps = 0.0, 0
-    n = 1  # the path is warm from the timed loop; model creation + upload are part of every call
-    for i in range(n):
+    tot, steps, per = 0.0, 0, []
+    for _ in range(n):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         mm = Model.from_arrays(d["x0"], d["rate"], d["col_ptr"], d["row_ind"], d["stoich"], pop_bits=m.pop_bits)
@@ -356,45 +428,42 @@ def e2e(args, wl, m, R, T, stream, sptr):
         dt = time.perf_counter() - t0
         tot += dt
         steps += r.leaps + r.ssa_steps
+        per.append((r.leaps + r.ssa_steps) / dt)
     return {"value": steps / tot, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-            "steps": n, "timing": "host wall clock around model upload + tl_simulate + statistics read-back"}
+            "steps": n, "samples": per,
+            "timing": "host wall clock around model upload + tl_simulate + statistics read-back, per sample"}
 
 
-def cpu_baseline(args, wl, m, R, budget_s: float = 12.0, check_gpu: bool = False):
+def cpu_baseline(o, wl, R, T, seed, budget_s: float = 12.0):
     """FP64 oracle port of the reference's algorithm on the host cores, on a
-    bounded sample (the first realizations of the same ensemble).  With
-    check_gpu the same realizations also run on the GPU for fp64_check."""
-    from oracle import py as ora
-    o = ora.OracleModel.from_desc(m.desc())
+    bounded sample (the first realizations of the same ensemble)."""
     cores = os.cpu_count() or 1
     n = cores
     t0 = time.perf_counter()
-    r = o.simulate(wl["t_final"], R, seed=args.seed, tracked=wl["tracked"], threads=cores, r_begin=0, r_end=n)
+    r = o.simulate(T, R, seed=seed, tracked=wl["tracked"], threads=cores, r_begin=0, r_end=n)
     dt = time.perf_counter() - t0
     done, steps = n, r["leaps"] + r["ssa_steps"]
     finals = [r["samples"][0, :, -1, :]]
     while dt < budget_s and done < R:
         k = min(R - done, max(cores, int(done * (budget_s - dt) / max(dt, 1e-3) * 0.8)))
         t1 = time.perf_counter()
-        r = o.simulate(wl["t_final"], R, seed=args.seed, tracked=wl["tracked"], threads=cores, r_begin=done,
-                       r_end=done + k)
+        r = o.simulate(T, R, seed=seed, tracked=wl["tracked"], threads=cores, r_begin=done, r_end=done + k)
         dt += time.perf_counter() - t1
         done += k
         steps += r["leaps"] + r["ssa_steps"]
         finals.append(r["samples"][0, :, -1, :])
-    out = {"value": steps / dt, "unit": UNIT, "cores": cores, "kind": "port",
-           "sample": f"{done} of {R} realizations of the same workload, FP64 oracle, {cores} threads, {dt:.1f} s"}
-    if check_gpu:
-        out["fp64_check"] = fp64_check(args, wl, m, done, np.concatenate(finals).astype(np.float64))
-    return out
+    return {"value": steps / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{done} of {R} realizations of the same workload, FP64 oracle, {cores} threads, {dt:.1f} s",
+            "_finals": np.concatenate(finals).astype(np.float64)}
 
 
-def fp64_check(args, wl, m, n, ora_final):
+def fp64_check(args, wl, m, ora_final):
     """Error of the engine against the FP64 oracle on the baseline's sample:
     the same n realizations (same ids, so the same Philox streams) run on
     the GPU with their samples kept.  Reports, per tracked species, the
     relative difference of the ensemble mean and variance at t_final and the
     share of realizations whose final state is identical."""
+    n = len(ora_final)
     g = m.simulate(wl["t_final"], n, seed=args.seed, tracked=wl["tracked"], keep_samples=True,
                    variant=args.variant)
     gf = g.samples[0, :, -1, :].astype(np.float64)
@@ -402,35 +471,38 @@ def fp64_check(args, wl, m, n, ora_final):
     var_o = ora_final.var(0, ddof=1) if n > 1 else np.zeros(gf.shape[1])
     var_g = gf.var(0, ddof=1) if n > 1 else np.zeros(gf.shape[1])
     rel_var = np.abs(var_g - var_o) / np.maximum(var_o, 1e-300)
-    # one standard error of each difference, were the two samples independent
-    se_mean = np.sqrt((var_g + var_o) / max(n, 1)) / np.maximum(np.abs(ora_final.mean(0)), 1e-300)
-    se_var = np.sqrt(4.0 / max(n - 1, 1)) * np.ones_like(rel_var)
-    return {"realizations": int(n), "tracked": wl["tracked"],
-            "mean_rel_err": [float(x) for x in rel_mean], "mean_rel_se": [float(x) for x in se_mean],
-            "var_rel_err": [float(x) for x in rel_var], "var_rel_se": [float(x) for x in se_var],
+    return {"realizations": int(n), "tracked": wl["tracked"], "paired": "same realization ids and streams",
+            "mean_rel_err": [float(x) for x in rel_mean], "var_rel_err": [float(x) for x in rel_var],
             "identical_final_state": float(np.mean(np.all(gf == ora_final, axis=1)))}
 
 
 def run_reference(args, wl, rank):
+    """The reference arm: the FP64 oracle port on all host cores, model built
+    by the oracle's own generator (the engine library is never loaded)."""
     if rank != 0:
         return
-    from tau_leaping_gb300 import Model
-    m = Model.generate(wl["family"])
-    R = args.realizations or wl["R"]
+    if wl["family"] == "batch":
+        print(json.dumps({"impl": "reference", "unavailable": "the batched sensitivity workload has no CPU "
+                                                             "counterpart in the reference"}), flush=True)
+        return
+    from oracle import py as ora
+    o = ora.OracleModel.from_desc(ora.generate(wl["family"]))
+    R, T = args.realizations or wl["R"], args.t_final or wl["t_final"]
     for _ in range(args.warmup):
-        cpu_baseline(args, wl, m, R, budget_s=2.0)
+        cpu_baseline(o, wl, R, T, args.seed, budget_s=2.0)
     vals, t_all = [], 0.0
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        cb = cpu_baseline(args, wl, m, R, budget_s=8.0)
+        cb = cpu_baseline(o, wl, R, T, args.seed, budget_s=8.0)
         t_all += time.perf_counter() - t0
         vals.append(cb["value"])
+    cb.pop("_finals")
     v = float(np.mean(vals))
     cb["value"] = v
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t_all / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp64+int64", "data": "synthetic (seeded generator)",
-            "config": {"workload": wl["desc"], "realizations_per_gpu": R, "t_final": wl["t_final"]},
+            "config": workload_config(wl, R, T, int(os.environ.get("WORLD_SIZE", "1"))),
             "impl": "reference", "cpu_baseline": cb,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -447,7 +519,7 @@ def main():
     ap.add_argument("--variant", type=int, default=0)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparisons")
     ap.add_argument("--batch-scale", type=float, default=1.0)
     ap.add_argument("--t-final", type=float, default=0.0, help="override t_final (profiling captures)")
     args = ap.parse_args()
@@ -457,11 +529,13 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    import __graft_entry__
-    __graft_entry__.build()
     if args.impl == "reference":
+        from oracle import build as ob
+        ob.build()
         run_reference(args, wl, rank)
         return
+    import __graft_entry__
+    __graft_entry__.build()
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl", device_id=torch.device(f"cuda:{local_rank}"))

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define TL_ABI_VERSION 1
+#define TL_ABI_VERSION 2
 
 typedef enum tl_status {
     TL_OK = 0,
@@ -45,7 +45,9 @@ typedef enum tl_status {
     TL_ERR_OUT_OF_MEMORY = 9,
     TL_ERR_IO = 10,              /* file could not be opened / written      */
     TL_ERR_PARSE = 11,           /* StochKit XML could not be parsed        */
-    TL_ERR_NUMERIC = 12          /* NaN / negative propensity or rate       */
+    TL_ERR_NUMERIC = 12          /* negative or non-finite rate, or a leap
+                                    still negative after max_halvings
+                                    halvings of tau                        */
 } tl_status;
 
 typedef struct tl_model tl_model;
@@ -220,6 +222,19 @@ typedef struct tl_run_cfg {
     int64_t realization_offset; /* first realization id of this call: a
                                    shard [off, off+n) of a larger ensemble
                                    draws the same streams as in one call   */
+    int32_t max_halvings;    /* a leap whose update leaves a population
+                                negative is rejected and retried with tau
+                                halved (Cao, Gillespie, Petzold 2006); a
+                                realization whose leap is still rejected
+                                after this many halvings stops and the call
+                                returns TL_ERR_NUMERIC.  0 = 64            */
+    int32_t stage_wait_polls; /* polls of the bounded wait for the model
+                                tables' copy into shared memory: 0 = 2^22;
+                                < 0 = none, so that the wait gives up at
+                                once and the call returns
+                                TL_ERR_WAIT_TIMEOUT (checks the timeout
+                                path; the copy is still drained before a
+                                CTA exits)                                 */
 } tl_run_cfg;
 
 /* Fill cfg with the reference's defaults (eps 0.03, 1 interval, ...). */
@@ -278,16 +293,15 @@ tl_status tl_simulate_batch(tl_batch_item *items, int32_t n_items,
  * tl_simulate without any device allocation.  No counterpart in the
  * reference (it allocates per realization with Thrust vectors).
  *
- * For callers that cannot call cudaMalloc: code that runs inside a CUDA
- * graph capture (cudaMalloc is not capturable), code whose GPU memory is
- * owned by a pool allocator that has already reserved the device, and
- * latency-bound loops that cannot afford cudaMalloc / cudaFree's implicit
- * device-wide synchronisation.  The caller passes inputs and outputs as
- * for tl_simulate; every piece of device scratch of the run (rate and
- * t_final tables, per-realization grid samples, counters, reduced
- * statistics) lives in one file-scope device array of
- * TL_STATIC_SCRATCH_BYTES that every GPU loading libtl.so holds until the
- * process exits.
+ * For callers that cannot call cudaMalloc: a host whose GPU memory is owned
+ * by a pool allocator that has already reserved the device, and
+ * latency-bound loops that cannot take cudaMalloc / cudaFree's implicit
+ * device-wide synchronisation.  The caller passes inputs and outputs as for
+ * tl_simulate; every piece of device scratch of the run (rate and t_final
+ * tables, per-realization grid samples, counters, reduced statistics, and
+ * the per-CTA state of models past shared memory) lives in one file-scope
+ * device array of TL_STATIC_SCRATCH_BYTES that every GPU loading libtl.so
+ * holds until the process exits.
  *  - The model's tables must already be on the device: any earlier
  *    tl_simulate / tl_eval_leap / tl_replay call on the model uploads them;
  *    otherwise TL_ERR_INVALID_ARGUMENT.
@@ -297,13 +311,14 @@ tl_status tl_simulate_batch(tl_batch_item *items, int32_t n_items,
  *    giving both sizes.  The plain form, sensitivities and the measured
  *    autotuner are not available here (TL_ERR_UNSUPPORTED / ignored).
  *  - The first call on a device looks up the array's device address
- *    (cudaGetSymbolAddress) with that device current; make that first call
- *    before any stream capture.
+ *    (cudaGetSymbolAddress) with that device current and keeps it for the
+ *    life of the process; make that first call before any stream capture,
+ *    and do not use the library across a cudaDeviceReset.
  *  - All calls share the one array, which keeps the last call's contents
  *    (counters are cleared at the start of each call).  Calls that overlap
  *    on the GPU - from two host threads, or on two streams - race on it.
- *  - res->kernel_ms is host-timed from launch to completion (no CUDA event
- *    is created).
+ *  - The call waits for its stream before it returns.  res->kernel_ms is
+ *    host-timed from launch to completion (no CUDA event is created).
  */
 #define TL_STATIC_SCRATCH_BYTES (16u << 20)
 tl_status tl_simulate_static(tl_model *m, const tl_run_cfg *cfg,

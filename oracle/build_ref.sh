@@ -1,11 +1,14 @@
 #!/usr/bin/env bash
 # Build the reference's own host-compilable functors into oracle/_ref/.
-#   usage: build_ref.sh <reference root> <output dir>
-# The reference's CUDA file is compiled where it lies (included by
+#   usage: build_ref.sh <output dir> [<reference root>]
+# The reference root defaults to where this container keeps the reference's
+# sources; without them the script does nothing (the GPU hosts never have
+# them).  The reference's CUDA file is compiled where it lies (included by
 # ref/harness.cpp) with g++ on Thrust's CPP backend; ref/shim.h supplies
 # what the 2012 code base expects from its toolchain.  Nothing is copied.
 set -euo pipefail
-REF="$1"; OUT="$2"
+OUT="$1"; REF="${2:-/root/reference}"
+[ -d "$REF/tau_leaping" ] || exit 0
 HERE="$(cd "$(dirname "$0")" && pwd)"
 CUDA_INC=/usr/local/cuda/include
 mkdir -p "$OUT"

@@ -42,6 +42,13 @@ def lib():
         L.ora_philox.argtypes = [P(C.c_uint32), P(C.c_uint32), C.c_int, P(C.c_uint32)]
         L.ora_poisson.argtypes = [P(C.c_double), C.c_int, C.c_uint64, C.c_uint32, C.c_int, P(C.c_int64)]
         L.ora_simulate.argtypes = [C.c_void_p, P(OraCfg), P(C.c_int64), P(C.c_double), P(C.c_int64)]
+        L.ora_gen_new.restype = C.c_void_p
+        L.ora_gen_new.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int64, C.c_int64, C.c_double, C.c_double,
+                                  C.c_double, C.c_double, C.c_uint64]
+        L.ora_gen_sizes.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int), P(C.c_int)]
+        L.ora_gen_copy.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_double), P(C.c_int32), P(C.c_int32),
+                                   P(C.c_int8)]
+        L.ora_gen_free.argtypes = [C.c_void_p]
         _lib = L
     return _lib
 
@@ -118,6 +125,42 @@ class OracleModel:
         del keep
         return {"samples": samples, "scores": scores, "leaps": int(cnt[0]), "ssa_steps": int(cnt[1]),
                 "rejections": int(cnt[2]), "truncated": int(cnt[3])}
+
+
+# The benchmark configurations' generator parameters per family (the same
+# defaults as the engine's tl_gen_params_init).
+GEN_FAMILIES = {"dimer": 1, "toy": 2, "chain": 3, "colloid": 4}
+GEN_DEFAULTS = {
+    "dimer": dict(n_species=3, n_channels=4, x0_min=100000, x0_max=100000, seed=1),
+    "toy": dict(n_species=128, n_channels=256, x0_min=0, x0_max=10000, rate_min=1e-3, rate_max=1.0, seed=7),
+    "chain": dict(n_species=1024, n_channels=1024, x0_min=1000, x0_max=2000, rate_min=1.0, rate_max=1.0, seed=11),
+    "colloid": dict(n_species=250, n_channels=31250, x0_min=1000, x0_max=2000, rate_assoc=1e-4, rate_dissoc=0.1,
+                    seed=13),
+}
+
+
+def generate(family: str, **kw) -> dict:
+    """Model description {x0, rate, col_ptr, row_ind, stoich} of a seeded
+    family, built by the oracle alone (no engine library)."""
+    g = dict(n_species=0, n_channels=0, x0_min=0, x0_max=0, rate_min=0.0, rate_max=0.0, rate_assoc=0.0,
+             rate_dissoc=0.0, seed=0)
+    g.update(GEN_DEFAULTS[family])
+    g.update(kw)
+    L = lib()
+    h = L.ora_gen_new(GEN_FAMILIES[family], g["n_species"], g["n_channels"], g["x0_min"], g["x0_max"],
+                      g["rate_min"], g["rate_max"], g["rate_assoc"], g["rate_dissoc"], g["seed"])
+    if not h:
+        raise ValueError(f"oracle generator rejected {family} {kw}")
+    try:
+        n, m, z = C.c_int(), C.c_int(), C.c_int()
+        L.ora_gen_sizes(h, C.byref(n), C.byref(m), C.byref(z))
+        d = {"x0": np.zeros(n.value, np.int64), "rate": np.zeros(m.value), "col_ptr": np.zeros(m.value + 1, np.int32),
+             "row_ind": np.zeros(z.value, np.int32), "stoich": np.zeros(z.value, np.int8)}
+        L.ora_gen_copy(h, _p(d["x0"], C.c_int64), _p(d["rate"], C.c_double), _p(d["col_ptr"], C.c_int32),
+                       _p(d["row_ind"], C.c_int32), _p(d["stoich"], C.c_int8))
+    finally:
+        L.ora_gen_free(h)
+    return d
 
 
 def philox(ctr, key) -> np.ndarray:

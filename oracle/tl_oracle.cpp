@@ -603,3 +603,174 @@ int ora_simulate(const ora_model* m, const ora_cfg* c, int64_t* samples, double*
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Workload models without the engine: the four seeded families of the
+// benchmark configurations, built here so that a CPU-only caller (the
+// reference arm of the benchmark) never loads the engine library.  The
+// draws follow the engine's generator's documented order and mappings
+// (std::mt19937_64; integers by 128-bit multiply-shift; reals from the top
+// 53 bits; rates rounded to 9 significant digits; channel structures, then
+// rates, then x0); tests check the two produce identical descriptions.
+// Channel structures: the dimerisation decay of the reference's
+// examples/dimer_decay.xml, the random toy network, the cyclic chain, and
+// colloidal aggregation in the channel order of
+// toy_system_gen/main.cpp:712-756.
+// ---------------------------------------------------------------------------
+#include <cstdio>
+#include <cstdlib>
+#include <map>
+#include <random>
+
+struct ora_gen {
+    std::vector<int64_t> x0;
+    std::vector<double> rate;
+    std::vector<int32_t> col_ptr{0}, row_ind;
+    std::vector<int8_t> stoich;
+};
+
+namespace {
+
+struct GenDraw {
+    std::mt19937_64 e;
+    int64_t in(int64_t lo, int64_t hi) {  // uniform integer in [lo, hi]
+        const unsigned __int128 n = (unsigned __int128)(uint64_t)(hi - lo) + 1u;
+        return lo + (int64_t)(uint64_t)(((unsigned __int128)e() * n) >> 64);
+    }
+    double unit() { return (double)(e() >> 11) / 9007199254740992.0; }
+};
+
+double sig9(double v) {
+    char s[48];
+    std::snprintf(s, sizeof s, "%.9g", v);
+    return std::strtod(s, nullptr);
+}
+
+// one channel: reactant and product species are distinct in every family,
+// so the column is the species sorted ascending, reactants negative
+void add_channel(ora_gen& g, const std::map<int, int>& entries) {
+    for (const auto& e : entries) {
+        g.row_ind.push_back(e.first);
+        g.stoich.push_back((int8_t)e.second);
+    }
+    g.col_ptr.push_back((int32_t)g.row_ind.size());
+}
+
+}  // namespace
+
+extern "C" {
+
+// family: 1 dimer, 2 toy, 3 chain, 4 colloid (the engine's numbering).
+// Returns nullptr for an unknown family or sizes the family rejects.
+ora_gen* ora_gen_new(int family, int N, int M, int64_t x0_min, int64_t x0_max, double rate_min, double rate_max,
+                     double rate_assoc, double rate_dissoc, uint64_t seed) {
+    ora_gen* g = new ora_gen();
+    GenDraw d{std::mt19937_64(seed)};
+    if (family == 1) {
+        const double c[4] = {1.0, 0.002, 0.5, 0.04};
+        add_channel(*g, {{0, -1}});
+        add_channel(*g, {{0, -2}, {1, 1}});
+        add_channel(*g, {{0, 2}, {1, -1}});
+        add_channel(*g, {{1, -1}, {2, 1}});
+        g->rate.assign(c, c + 4);
+        g->x0 = {x0_max, 0, 0};
+    } else if (family == 2) {
+        if (N < 4 || M < 1) {
+            delete g;
+            return nullptr;
+        }
+        std::vector<int> pool(N);
+        for (int i = 0; i < N; ++i) pool[i] = i;
+        // species from the not-yet-used pool first, then uniformly
+        auto take = [&]() {
+            if (pool.empty()) return (int)d.in(0, N - 1);
+            const size_t k = (size_t)d.in(0, (int64_t)pool.size() - 1);
+            std::swap(pool[k], pool.back());
+            const int s = pool.back();
+            pool.pop_back();
+            return s;
+        };
+        auto take_new = [&](const std::map<int, int>& have) {
+            for (int t = 0; t < 1000; ++t) {
+                const int s = take();
+                if (!have.count(s)) return s;
+            }
+            for (int s = 0; s < N; ++s)
+                if (!have.count(s)) return s;
+            return 0;
+        };
+        for (int j = 0; j < M; ++j) {
+            std::map<int, int> col;
+            const bool two = d.in(0, 1) == 1;
+            const int a = take();
+            if (!two) {
+                col[a] = -(1 + (int)d.in(0, 1));
+            } else {
+                col[a] = -1;
+                const int b = take_new(col);
+                col[b] = -1;
+            }
+            const int np = 1 + (int)d.in(0, 1);
+            for (int q = 0; q < np; ++q) {
+                const int p = take_new(col);
+                col[p] = 1 + (int)d.in(0, 1);
+            }
+            add_channel(*g, col);
+        }
+        const double l0 = std::log10(rate_min), l1 = std::log10(rate_max);
+        for (int j = 0; j < M; ++j) g->rate.push_back(sig9(std::pow(10.0, l0 + (l1 - l0) * d.unit())));
+        for (int i = 0; i < N; ++i) g->x0.push_back(d.in(x0_min, x0_max));
+    } else if (family == 3) {
+        if (N < 2) {
+            delete g;
+            return nullptr;
+        }
+        for (int i = 0; i < N; ++i) {
+            add_channel(*g, {{i, -1}, {(i + 1) % N, 1}});
+            g->rate.push_back(sig9(rate_min));
+        }
+        for (int i = 0; i < N; ++i) g->x0.push_back(d.in(x0_min, x0_max));
+    } else if (family == 4) {
+        if (N < 2) {
+            delete g;
+            return nullptr;
+        }
+        // S_k is index k-1: association n + m -> n + m (m >= n), then
+        // dissociation p -> q + (p - q), q <= p / 2
+        for (int n = 1; 2 * n <= N; ++n)
+            for (int m = n; m <= N - n; ++m) {
+                if (m == n) add_channel(*g, {{n - 1, -2}, {2 * n - 1, 1}});
+                else add_channel(*g, {{n - 1, -1}, {m - 1, -1}, {n + m - 1, 1}});
+                g->rate.push_back(sig9(rate_assoc));
+            }
+        for (int p = 1; p <= N; ++p)
+            for (int q = 1; 2 * q <= p; ++q) {
+                if (2 * q == p) add_channel(*g, {{p - 1, -1}, {q - 1, 2}});
+                else add_channel(*g, {{p - 1, -1}, {q - 1, 1}, {p - q - 1, 1}});
+                g->rate.push_back(sig9(rate_dissoc));
+            }
+        for (int i = 0; i < N; ++i) g->x0.push_back(d.in(x0_min, x0_max));
+    } else {
+        delete g;
+        return nullptr;
+    }
+    return g;
+}
+
+void ora_gen_sizes(const ora_gen* g, int* N, int* M, int* nnz) {
+    *N = (int)g->x0.size();
+    *M = (int)g->rate.size();
+    *nnz = (int)g->row_ind.size();
+}
+
+void ora_gen_copy(const ora_gen* g, int64_t* x0, double* rate, int32_t* col_ptr, int32_t* row_ind, int8_t* stoich) {
+    std::copy(g->x0.begin(), g->x0.end(), x0);
+    std::copy(g->rate.begin(), g->rate.end(), rate);
+    std::copy(g->col_ptr.begin(), g->col_ptr.end(), col_ptr);
+    std::copy(g->row_ind.begin(), g->row_ind.end(), row_ind);
+    std::copy(g->stoich.begin(), g->stoich.end(), stoich);
+}
+
+void ora_gen_free(ora_gen* g) { delete g; }
+
+}  // extern "C"

@@ -65,7 +65,7 @@ class RunCfg(C.Structure):
                 ("n_rate_sets", c_i32), ("rate_sets", P(c_dbl)), ("t_final_sets", P(c_dbl)),
                 ("variant", c_i32), ("block_threads", c_i32), ("flags", c_u32), ("n_critical", c_i32),
                 ("ssa_factor", c_i32), ("ssa_block", c_i32), ("max_steps", c_i64), ("stream", c_vp),
-                ("realization_offset", c_i64)]
+                ("realization_offset", c_i64), ("max_halvings", c_i32), ("stage_wait_polls", c_i32)]
 
 
 class Result(C.Structure):

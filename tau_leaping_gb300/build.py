@@ -1,5 +1,5 @@
-"""Build the engine in-tree: libtl.so (CUDA kernels + C ABI), the tl_cli and
-tl_gen executables, and the oracle's C++ library.
+"""Build the engine in-tree: libtl.so (CUDA kernels + C ABI) and the tl_cli
+and tl_gen executables.
 
 Every CUDA translation unit is compiled for sm_103a only
 (``-gencode arch=compute_103a,code=sm_103a``); translation units are compiled
@@ -105,17 +105,6 @@ def _build_lib() -> Path:
     return LIB
 
 
-def build_oracle() -> Path:
-    sys.path.insert(0, str(ROOT))
-    from oracle import build as ob  # noqa: E402  (oracle recipe lives beside the oracle)
-    return ob.build()
-
-
-def build_all() -> None:
-    build_lib()
-    build_oracle()
-
-
 if __name__ == "__main__":
-    build_all()
+    build_lib()
     print("built", LIB)

@@ -465,6 +465,8 @@ static tl_status job_bind(Job& J, unsigned char* B, cudaStream_t st) {
     p.scores = rb.scores;
     p.max_steps = cfg->max_steps;
     p.flags = cfg->flags;
+    p.max_halv = cfg->max_halvings > 0 ? cfg->max_halvings : 64;
+    p.wait_polls = cfg->stage_wait_polls == 0 ? (1 << 22) : std::max(cfg->stage_wait_polls, 0);
     p.blob = m->d.blob;
     p.stage_bytes = J.pl.stage;
     p.off_chan = m->d.off_chan;
@@ -558,7 +560,8 @@ static tl_status job_finish(Job& J, double kernel_ms, int launches, double total
         return TL_ERR_OVERFLOW;
     }
     if (eb & (kErrHalving | kErrNumeric)) {
-        set_last_error("a leap could not be made non-negative by halving tau");
+        set_last_error("a leap could not be made non-negative by halving tau " +
+                       std::to_string(J.p.max_halv) + " times (max_halvings)");
         return TL_ERR_NUMERIC;
     }
     if (J.hc[4] > 0) {
@@ -1399,7 +1402,9 @@ static __device__ __align__(256) unsigned char g_static_scratch[TL_STATIC_SCRATC
 
 // Device address of g_static_scratch per device ordinal.  In host code the
 // array's name is only a host-side stand-in, never a device address: the
-// address is looked up once per device, with that device current.
+// address is looked up once per device, with that device current, and kept
+// for the life of the process (so the library must not be used across a
+// cudaDeviceReset, which would unmap it).
 static std::mutex g_static_mu;
 static void* g_static_addr[256];
 
@@ -1445,7 +1450,7 @@ extern "C" tl_status tl_simulate_static(tl_model* m, const tl_run_cfg* cfg, tl_r
     TLC(cudaSetDevice(m->d.device));
     cudaStream_t st = (cudaStream_t)cfg->stream;
     ps = make_plan(m, cfg->variant, cfg->block_threads, J.mode, J.compat_stoich,
-                   (cfg->flags & TL_FLAG_NO_STAGE) != 0, J.total, J.pl);
+                   (cfg->flags & TL_FLAG_NO_STAGE) != 0, J.total, J.pl, (cfg->flags & TL_FLAG_GLOBAL_SLOTS) != 0);
     if (ps != TL_OK) return ps;
     Carver c;
     job_layout(J, c);

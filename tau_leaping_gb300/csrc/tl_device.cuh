@@ -35,7 +35,7 @@ constexpr float kInfF = __builtin_huge_valf();
 enum : unsigned {
     kErrOverflow = 1u << 0,
     kErrWaitTimeout = 1u << 1,
-    kErrHalving = 1u << 2,    // leap halved 64 times without success
+    kErrHalving = 1u << 2,    // leap still rejected after max_halv halvings
     kErrNumeric = 1u << 3,
     kErrStage = 1u << 4,
 };
@@ -639,6 +639,8 @@ struct SimParams {
     float* scores;      // [S*R][M] when sensitivity is on
     long long max_steps;
     unsigned flags;
+    int max_halv;       // tau halvings allowed per leap before the realization stops
+    int wait_polls;     // polls of the bounded staging wait (0: give up at once)
     // staging of the constant blob into shared memory
     const unsigned char* blob;
     int stage_bytes;    // 0 = no staging
@@ -1149,7 +1151,7 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
         g.sync();
         pass_props<Grp, Pop, COMPAT>(g, p, mv, rate, s.x, s.a, pa, pac);
         g.sync();
-        if (attempt >= 64) {
+        if (attempt + 1 > p.max_halv) {
             if (g.leader()) atomicOr((unsigned*)(p.ctr + 5), kErrHalving);
             st.done = 1;
             while (st.kpt <= p.n_int) record_point<Grp, Pop>(g, p, s.x, samp, st.kpt++);

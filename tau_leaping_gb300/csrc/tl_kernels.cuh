@@ -50,9 +50,12 @@ TL_D bool mbar_try_wait(uint32_t bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Stage p.stage_bytes of the constant blob into dst; bounded wait.  Returns
-// false (CTA-uniform) if the copy did not complete within the limit.
-TL_D bool stage_blob(unsigned char* dst, const SimParams& p, unsigned long long* bar) {
+// Stage `bytes` of the constant blob into dst with a bounded wait of
+// `polls` mbarrier polls.  Returns false (CTA-uniform) if the copy did not
+// complete within them; the copies still in flight into this CTA's shared
+// memory are then drained (again bounded) before the caller lets the CTA
+// exit.
+TL_D bool stage_blob(unsigned char* dst, const unsigned char* src, int bytes, int polls, unsigned long long* bar) {
     const uint32_t ba = smem_u32(bar), da = smem_u32(dst);
     if (threadIdx.x == 0) {
         mbar_init(ba, 1);
@@ -60,23 +63,25 @@ TL_D bool stage_blob(unsigned char* dst, const SimParams& p, unsigned long long*
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        mbar_expect_tx(ba, (uint32_t)p.stage_bytes);
+        mbar_expect_tx(ba, (uint32_t)bytes);
         constexpr int kChunk = 32768;
-        for (int off = 0; off < p.stage_bytes; off += kChunk) {
-            const int n = p.stage_bytes - off < kChunk ? p.stage_bytes - off : kChunk;
-            bulk_g2s(da + off, p.blob + off, (uint32_t)n, ba);
+        for (int off = 0; off < bytes; off += kChunk) {
+            const int n = bytes - off < kChunk ? bytes - off : kChunk;
+            bulk_g2s(da + off, src + off, (uint32_t)n, ba);
         }
     }
     bool ok = false;
-    for (int it = 0; it < (1 << 22); ++it) {
+    for (int it = 0; it < polls; ++it) {
         if (mbar_try_wait(ba, 0)) {
             ok = true;
             break;
         }
     }
     if (!ok) {
-        // give the copies in flight one more bounded chance before leaving
-        for (int it = 0; it < (1 << 22) && !ok; ++it) ok = mbar_try_wait(ba, 0);
+        // gave up: drain the copies before anything else reuses or releases
+        // this shared memory
+        for (int it = 0; it < (1 << 22); ++it)
+            if (mbar_try_wait(ba, 0)) break;
     }
     return __syncthreads_and(ok ? 1 : 0) != 0;
 }
@@ -213,7 +218,7 @@ __global__ void __launch_bounds__(KIND == 0 ? 1024 : 256, KIND == 0 ? 1 : KIND =
     MView mv = p.g;
     unsigned char* slots = smem;
     if (p.stage_bytes > 0) {
-        if (!stage_blob(smem, p, &mbar)) {
+        if (!stage_blob(smem, p.blob, p.stage_bytes, p.wait_polls, &mbar)) {
             if (threadIdx.x == 0) atomicOr((unsigned*)(p.ctr + 5), kErrWaitTimeout | kErrStage);
             return;
         }
@@ -257,10 +262,7 @@ __global__ void __launch_bounds__(256, TL_BATCH_MINB) k_batch(BatchParams bp) {
     __shared__ __align__(8) unsigned long long mbar;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     if (bp.stage_bytes > 0) {
-        SimParams sp0{};
-        sp0.blob = bp.stage_src;
-        sp0.stage_bytes = bp.stage_bytes;
-        if (!stage_blob(smem, sp0, &mbar)) {
+        if (!stage_blob(smem, bp.stage_src, bp.stage_bytes, bp.items[0].p.wait_polls, &mbar)) {
             if (threadIdx.x == 0) atomicOr((unsigned*)(bp.items[0].p.ctr + 5), kErrWaitTimeout | kErrStage);
             return;
         }

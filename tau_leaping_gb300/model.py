@@ -130,7 +130,8 @@ class Model:
 
     # ---- hot path -----------------------------------------------------
     def _cfg(self, t_final, n, seed, intervals, tracked, eps, variant, flags, rate_sets, t_final_sets,
-             max_steps, block_threads, stream, n_critical=0, ssa_factor=0, ssa_block=0, realization_offset=0):
+             max_steps, block_threads, stream, n_critical=0, ssa_factor=0, ssa_block=0, realization_offset=0,
+             max_halvings=0, stage_wait_polls=0):
         cfg = F.RunCfg()
         F.lib().tl_run_cfg_init(C.byref(cfg))
         cfg.t_final = float(t_final)
@@ -161,6 +162,8 @@ class Model:
         cfg.ssa_block = int(ssa_block)
         cfg.stream = stream
         cfg.realization_offset = int(realization_offset)
+        cfg.max_halvings = int(max_halvings)
+        cfg.stage_wait_polls = int(stage_wait_polls)
         return cfg, keep
 
     def simulate(self, t_final: float, n: int, seed: int = 1, intervals: int = 1, tracked=None,

@@ -7,7 +7,6 @@ import pytest
 ROOT = Path(__file__).resolve().parents[1]
 sys.path.insert(0, str(ROOT))
 
-REFERENCE = Path(os.environ.get("TL_REFERENCE_DIR", "/root/reference"))
 
 
 def pytest_configure(config):
@@ -38,14 +37,19 @@ def pytest_collection_modifyitems(config, items):
 @pytest.fixture(scope="session", autouse=True)
 def _built():
     """Build libtl.so and the oracle once per session (in-tree, incremental)."""
+    from oracle import build as ob
     from tau_leaping_gb300 import build
     build.build_lib()
-    build.build_oracle()
+    ob.build()
     yield
 
 
 @pytest.fixture(scope="session")
-def reference_dir():
-    if not (REFERENCE / "tau_leaping").is_dir():
-        pytest.skip("reference sources not present")
-    return REFERENCE
+def reference_build():
+    """The reference's own host build (oracle/_ref), present only where its
+    sources were available to the oracle's build recipe."""
+    lib = ROOT / "oracle" / "_ref" / "libtlref.so"
+    from oracle.build import native_elf
+    if not native_elf(lib):
+        pytest.skip("the reference's host build is not present")
+    return lib

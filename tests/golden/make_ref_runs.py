@@ -3,7 +3,10 @@ reference's own simulation (its Model API, host-built by
 oracle/build_ref.sh, logging on), for the statistical comparison of the
 engine's reference-compatibility mode with the reference's run.
 
-    python tests/golden/make_ref_runs.py
+    python tests/golden/make_ref_runs.py <reference root>
+
+(the reference root is the checkout whose oracle/_ref build this uses; it
+supplies examples/test_128.xml; TL_REFERENCE_DIR may give it instead)
 
 Models are those on which the reference is well defined (as many channels
 as species, so its FireReactions loop bound is right):
@@ -16,6 +19,7 @@ stored; the reference's own timing is kept for the record.
 """
 from __future__ import annotations
 
+import os
 import subprocess
 import sys
 import tempfile
@@ -25,7 +29,6 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
-REFERENCE = Path("/root/reference")
 
 RUNS = {
     # name: (model source, t_final, realizations, intervals, eps, tracked names)
@@ -60,6 +63,11 @@ def run(name, model_path, T, n, intervals, eps, tracked):
 def main():
     from oracle import build
     from tau_leaping_gb300 import Model
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TL_REFERENCE_DIR")
+    if not ref:
+        sys.exit("usage: make_ref_runs.py <reference root>")
+    REFERENCE = Path(ref)
+    os.environ["TL_REFERENCE_DIR"] = str(REFERENCE)
     build.build()
     out = {}
     with tempfile.TemporaryDirectory() as td:

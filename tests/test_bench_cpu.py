@@ -1,6 +1,7 @@
 """bench.py's host-side figures (no GPU): the algorithmic bytes per
-realization-step that the roofline divides by, and the DRAM traffic it reads
-from the committed ncu summaries."""
+realization-step that the roofline divides by, the config both arms report,
+and the rule that ncu figures are used only from the same kernel build."""
+import json
 import sys
 from pathlib import Path
 
@@ -18,13 +19,31 @@ def test_algorithmic_bytes_per_step_match_the_design_table():
         assert bench.alg_bytes_per_step(Model.generate(fam)) == b, fam
 
 
-def test_profile_traffic_is_read_from_the_committed_summaries():
-    for w in ("toy", "chain", "colloid", "dimer"):
-        t = bench.profile_traffic(w)
-        assert t is not None and t > 0, w
-    assert bench.profile_traffic("no-such-workload") is None
-
-
-def test_every_workload_has_a_description():
+def test_workload_sizes_match_the_generator():
     for name, wl in bench.WORKLOADS.items():
         assert wl["desc"] and wl["family"], name
+        if wl["family"] == "batch":
+            continue
+        m = Model.generate(wl["family"])
+        assert (m.n_species, m.n_channels, m.pop_bits) == (wl["n_species"], wl["n_channels"], wl["pop_bits"]), name
+        assert bench.dtype_of(wl) == ("fp32+int64" if m.pop_bits == 64 else "fp32+int32")
+
+
+def test_both_arms_report_the_same_config():
+    wl = bench.WORKLOADS["toy"]
+    a = bench.workload_config(wl, wl["R"], wl["t_final"], 1)
+    b = bench.workload_config(wl, wl["R"], wl["t_final"], 1)
+    assert a == b and json.dumps(a) == json.dumps(b)
+
+
+def test_ncu_record_is_used_only_for_the_same_kernel_build(tmp_path, monkeypatch):
+    monkeypatch.setattr(bench, "ROOT", tmp_path)
+    (tmp_path / "profiles").mkdir()
+    assert bench.ncu_record("k_fused_toy")[0] is None
+    rec = {"source_sha256": bench.kernel_source_hash(), "dram_bytes_per_launch": 5, "issue_slots_busy_pct": 70.0}
+    (tmp_path / "profiles" / "k_fused_toy.ncu.json").write_text(json.dumps(rec))
+    assert bench.ncu_record("k_fused_toy")[0]["dram_bytes_per_launch"] == 5
+    rec["source_sha256"] = "0" * 64
+    (tmp_path / "profiles" / "k_fused_toy.ncu.json").write_text(json.dumps(rec))
+    got, why = bench.ncu_record("k_fused_toy")
+    assert got is None and "another kernel build" in why

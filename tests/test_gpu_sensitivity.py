@@ -79,3 +79,81 @@ def test_lr_gradient_toy_network_channels():
         fd, fd_se = crn_fd(m, base, int(j), T, R, seed=12, tracked=[0])
         lr, lr_se = g["grad"][0, 0, j], g["stderr"][0, 0, j]
         assert abs(lr - fd[0]) <= 3 * np.hypot(lr_se, fd_se[0]), (j, lr, lr_se, fd[0], fd_se[0])
+
+
+@pytest.mark.slow
+def test_c5_full_configuration_gradients_per_set(capsys):
+    """The sensitivity + uneven-batch configuration in full, in one
+    tl_simulate_batch launch with sensitivities: the dimerisation decay
+    (S1 = 1e5) with 64 rate sets c_j * lognormal(0, 0.2) (seed 17), 4096
+    realizations each, t_final uniform in [1, 10]; the 128 x 256 toy network
+    with 16 sets, 1024 realizations each, t_final uniform in [0.05, 0.1].
+
+    For every one of the 80 sets, the likelihood-ratio gradient
+    dE[S_k(T)]/dc_j of each tracked species is compared with common-random-
+    number central finite differences (h = 1e-2 relative; the up and down
+    runs of a pair draw the same streams): every channel of the dimer, and
+    for the toy network the four channels of that set with the largest
+    |gradient| / standard error plus channels 0 and 128.  z = (LR - FD) /
+    (combined standard error).  With 704 comparisons some |z| > 3 are
+    expected by chance (about 1.9 for unbiased estimators), so the check
+    is: at most 1 % of the comparisons beyond 3 standard errors, none beyond
+    4.5 (a family-wise level of 0.5 %), and a mean z^2 near 1."""
+    from tau_leaping_gb300.model import simulate_batch
+    h = 1e-2
+    rng = np.random.default_rng(17)
+    dim, toy = Model.generate("dimer"), Model.generate("toy")
+    ds = dim.desc()["rate"][None, :] * rng.lognormal(0.0, 0.2, size=(64, 4))
+    dt = rng.uniform(1.0, 10.0, size=64)
+    ts = toy.desc()["rate"][None, :] * rng.lognormal(0.0, 0.2, size=(16, toy.n_channels))
+    tt = rng.uniform(0.05, 0.1, size=16)
+    lr = simulate_batch([
+        dict(model=dim, t_final=10.0, n=4096, seed=1, tracked=[0, 1], rate_sets=ds, t_final_sets=dt,
+             sensitivity=True),
+        dict(model=toy, t_final=0.1, n=1024, seed=1, tracked=[0, 4], rate_sets=ts, t_final_sets=tt,
+             sensitivity=True)])
+
+    def fd_pairs(m, sets, tf, pairs, R, tracked):
+        up, dn = [], []
+        for s, j in pairs:
+            u, d = sets[s].copy(), sets[s].copy()
+            u[j] *= 1 + h
+            d[j] *= 1 - h
+            up.append(u)
+            dn.append(d)
+        tfr = np.array([tf[s] for s, _ in pairs])
+        kw = dict(seed=77, tracked=tracked, keep_samples=True, t_final_sets=tfr)
+        a = m.simulate(float(tfr.max()), R, rate_sets=np.array(up), **kw).samples[:, :, -1, :].astype(float)
+        b = m.simulate(float(tfr.max()), R, rate_sets=np.array(dn), **kw).samples[:, :, -1, :].astype(float)
+        c = np.array([sets[s][j] for s, j in pairs])
+        d = (a - b) / (2 * h * c[:, None, None])               # [pairs, R, K]
+        return d.mean(1), d.std(1, ddof=1) / np.sqrt(R)
+
+    def zscore(diff, se):
+        # both estimates exactly zero (a channel that moves nothing): agreement
+        return diff / se if se > 0 else (0.0 if diff == 0 else np.inf)
+
+    z_all = {}
+    dpairs = [(s, j) for s in range(64) for j in range(4)]
+    fd, fse = fd_pairs(dim, ds, dt, dpairs, 4096, [0, 1])
+    g, gse = lr[0]["grad"], lr[0]["stderr"]                     # [S, K, M]
+    z_all["dimer"] = np.array([zscore(g[s, k, j] - fd[q, k], np.hypot(gse[s, k, j], fse[q, k]))
+                               for q, (s, j) in enumerate(dpairs) for k in range(2)])
+    g, gse = lr[1]["grad"], lr[1]["stderr"]
+    tpairs = []
+    for s in range(16):
+        score = np.max(np.abs(g[s]) / np.maximum(gse[s], 1e-300), axis=0)
+        pick = list(np.argsort(-score)[:4]) + [0, 128]
+        tpairs += [(s, int(j)) for j in dict.fromkeys(pick)]
+    fd, fse = fd_pairs(toy, ts, tt, tpairs, 1024, [0, 4])
+    z_all["toy"] = np.array([zscore(g[s, k, j] - fd[q, k], np.hypot(gse[s, k, j], fse[q, k]))
+                             for q, (s, j) in enumerate(tpairs) for k in range(2)])
+    z = np.concatenate(list(z_all.values()))
+    with capsys.disabled():
+        for name, zz in z_all.items():
+            print(f"\nC5 {name}: {len(zz)} LR-vs-CRN-FD comparisons, max |z| {np.abs(zz).max():.2f}, "
+                  f"{np.mean(np.abs(zz) > 3):.2%} beyond 3 s.e., mean z^2 {np.mean(zz ** 2):.2f}")
+    assert np.all(np.isfinite(z))
+    assert np.mean(np.abs(z) > 3) <= 0.01, np.sort(np.abs(z))[-10:]
+    assert np.abs(z).max() <= 4.5, np.abs(z).max()
+    assert 0.5 <= np.mean(z ** 2) <= 1.5, np.mean(z ** 2)

@@ -190,27 +190,32 @@ def test_colloid_cta_matches_oracle():
 
 def test_colloid_full_config_within_1pct_of_fp64_oracle(capsys):
     """Colloidal aggregation, 250 species x 31250 channels, int64, t_final
-    0.01, 4096 realizations (the full configuration): the ensemble mean and
-    variance of every species agree with the FP64 oracle running the same
-    method within 1 % plus four combined standard errors; the errors are
-    reported."""
+    0.01, 4096 realizations (the full configuration), compared realization
+    by realization with the FP64 oracle running the same method: both draw
+    realization r from the same Philox stream (same seed, same realization
+    ids), so the pairs differ only where FP32 and FP64 arithmetic pick a
+    different Poisson count.  The ensemble mean and the variance of every
+    species agree within 1 %; the errors are printed.  A second, independent
+    oracle ensemble (another seed) checks the statistics at 99 % on two
+    species."""
     m = Model.generate("colloid")
     N = m.n_species
     g = m.simulate(0.01, 4096, seed=13, tracked=list(range(N)), keep_samples=True)
     o = ora.OracleModel.from_desc(m.desc())
-    r = o.simulate(0.01, 4096, seed=14, tracked=list(range(N)), threads=8)
+    r = o.simulate(0.01, 4096, seed=13, tracked=list(range(N)), threads=16)
     a, b = g.samples[0, :, -1, :].astype(float), r["samples"][0, :, -1, :].astype(float)
     ma, mb, va, vb = a.mean(0), b.mean(0), a.var(0, ddof=1), b.var(0, ddof=1)
     rel_m = np.abs(ma - mb) / mb
     rel_v = np.abs(va - vb) / vb
-    se_m = np.sqrt(va / len(a) + vb / len(b)) / mb
-    se_v = np.sqrt(2.0 / (len(a) - 1) + 2.0 / (len(b) - 1))
+    same = np.mean(np.all(a == b, axis=1))
     with capsys.disabled():
-        print(f"\ncolloid-250 vs FP64 oracle (4096 + 4096 realizations): mean rel err max {rel_m.max():.2e} "
-              f"rms {np.sqrt((rel_m ** 2).mean()):.2e} (s.e. ~{np.median(se_m):.1e}); variance rel err max "
-              f"{rel_v.max():.2e} rms {np.sqrt((rel_v ** 2).mean()):.2e} (s.e. ~{se_v:.1e})")
-    assert np.all(rel_m <= 0.01 + 4 * se_m), rel_m.max()
-    assert np.all(rel_v <= 0.01 + 4 * se_v), rel_v.max()
+        print(f"\ncolloid-250 vs FP64 oracle, 4096 paired realizations: mean rel err max {rel_m.max():.2e} "
+              f"rms {np.sqrt((rel_m ** 2).mean()):.2e}; variance rel err max {rel_v.max():.2e} "
+              f"rms {np.sqrt((rel_v ** 2).mean()):.2e}; {same:.1%} of final states identical")
+    assert rel_m.max() <= 0.01, rel_m.max()
+    assert rel_v.max() <= 0.01, rel_v.max()
+    ind = o.simulate(0.01, 2048, seed=14, tracked=[0, 9], threads=16)["samples"][0, :, -1, :]
+    compare_final(a[:, [0, 9]], ind, "colloid-250 independent oracle ensemble")
 
 
 def test_state_larger_than_shared_memory_runs_from_global_slots():

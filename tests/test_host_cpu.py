@@ -25,7 +25,7 @@ def test_library_exports_every_declared_symbol():
     for n in names:
         assert hasattr(lib, n), f"libtl.so does not export {n}"
     assert set(names) == set(_ffi.SIGNATURES), "binding table out of sync with include/tl.h"
-    assert lib.tl_abi_version() == 1
+    assert lib.tl_abi_version() == 2
     for s in range(13):
         assert lib.tl_status_str(s)
 

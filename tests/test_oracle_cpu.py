@@ -68,7 +68,7 @@ def test_oracle_matches_reference_functors(gold, name):
         assert np.array_equal(fired[0], gold[f"{name}/fired_as_shipped"])
 
 
-def test_oracle_against_live_reference(reference_dir):
+def test_oracle_against_live_reference(reference_build):
     """Fresh random states through the reference's functors (oracle/_ref)."""
     import ctypes as C
 
@@ -117,3 +117,17 @@ def test_oracle_ssa_matches_exact_chain_solution():
     assert np.all(np.abs(x.mean(0) - mean) <= 4 * se)
     sev = var * np.sqrt(2.0 / len(x))
     assert np.all(np.abs(x.var(0, ddof=1) - var) <= 4.5 * sev)
+
+
+@pytest.mark.parametrize("family,kw", [("dimer", {}), ("toy", {}), ("chain", {}), ("colloid", {}),
+                                       ("toy", dict(n_species=16, n_channels=32, seed=3, x0_min=0, x0_max=60)),
+                                       ("colloid", dict(n_species=60)), ("chain", dict(n_species=48))])
+def test_oracle_generator_equals_engine_generator(family, kw):
+    """The oracle builds the benchmark models on its own (the CPU reference
+    arm never loads the engine): the same description as the engine's
+    seeded generator, array for array."""
+    from tau_leaping_gb300 import Model
+    a = ora.generate(family, **kw)
+    b = Model.generate(family, **kw).desc()
+    for k in ("x0", "rate", "col_ptr", "row_ind", "stoich"):
+        assert np.array_equal(a[k], b[k]), k

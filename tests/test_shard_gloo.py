@@ -1,12 +1,15 @@
-"""Multi-process path on CPU: two gloo ranks each run a contiguous shard of
-the realizations (the FP64 oracle stands in for the per-rank engine, which
-needs a GPU) and merge moments with tl_merge_moments; the result must equal
+"""Multi-process path: two gloo ranks each run a contiguous shard of the
+realizations and merge moments with tl_merge_moments; the result must equal
 one process running every realization, because streams are keyed by the
-realization id."""
+realization id.  On CPU the FP64 oracle stands in for the per-rank engine;
+where a GPU is present, a second test runs the engine itself in each rank
+(both ranks on the one GPU: their launches are independent, nothing in one
+waits on the other)."""
 import os
 import socket
 
 import numpy as np
+import pytest
 import torch.distributed as dist
 import torch.multiprocessing as mp
 
@@ -91,3 +94,48 @@ def test_two_gloo_ranks_equal_one_process():
         assert np.allclose(sd, full_sd, rtol=1e-10)
         # realization streams do not depend on the partition
         assert np.array_equal(samp, full_samp[off:off + cnt])
+
+
+def _engine_worker(rank, world, port, out):
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from tau_leaping_gb300 import Model
+    from tau_leaping_gb300.shard import simulate_sharded
+    m = Model.generate("toy", n_species=32, n_channels=64, seed=4, x0_max=3000)
+    keep = {}
+
+    def run(off, cnt):
+        r = m.simulate(0.004, cnt, seed=SEED, intervals=2, tracked=[0, 1], keep_samples=True,
+                       realization_offset=off)
+        keep["samp"] = r.samples[0]
+        return r.mean[0], r.stddev[0]
+
+    n, mean, sd = simulate_sharded(run, 1001)
+    out[rank] = (n, mean, sd, keep["samp"], shard_range(1001, world, rank))
+    dist.destroy_process_group()
+
+
+@pytest.mark.gpu
+def test_two_gloo_ranks_running_the_engine_equal_one_call():
+    from tau_leaping_gb300 import Model
+    world = 2
+    port = _free_port()
+    ctx = mp.get_context("spawn")
+    with ctx.Manager() as man:
+        out = man.dict()
+        procs = [ctx.Process(target=_engine_worker, args=(r, world, port, out)) for r in range(world)]
+        for p in procs:
+            p.start()
+        for p in procs:
+            p.join(300)
+            assert p.exitcode == 0
+        res = dict(out)
+    m = Model.generate("toy", n_species=32, n_channels=64, seed=4, x0_max=3000)
+    full = m.simulate(0.004, 1001, seed=SEED, intervals=2, tracked=[0, 1], keep_samples=True)
+    for rank in range(world):
+        n, mean, sd, samp, (off, cnt) = res[rank]
+        assert n == 1001
+        assert np.allclose(mean, full.mean[0], rtol=1e-12)
+        assert np.allclose(sd, full.stddev[0], rtol=1e-9)
+        assert np.array_equal(samp, full.samples[0, off:off + cnt])
