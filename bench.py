@@ -161,8 +161,8 @@ def model_bytes(m) -> tuple[int, int]:
     N, M, nn, nr = m.n_species, m.n_channels, m.nnz_net, m.nnz_raw
     a16 = lambda b: (b + 15) // 16 * 16  # noqa: E731
     w = 8 if m.pop_bits == 64 else 4
-    blob = (a16(16 * M) + a16(N) + a16(4 * N) + a16(4 * (N + 1)) + a16(4 * nn) + a16(4 * (M + 1)) + a16(4 * nn) +
-            a16(4 * (N + 1)) + a16(4 * nr))
+    blob = (a16(8 * M) + a16(M) + a16(N) + a16(4 * N) + a16(4 * (N + 1)) + a16(4 * nn) + a16(4 * (M + 1)) +
+            a16(4 * nn) + a16(4 * (N + 1)) + a16(4 * nr))
     return blob + N * w + 4 * M, w
 
 
@@ -174,7 +174,7 @@ def kernel_source_hash() -> str:
     for p in sorted(b.CSRC.glob("*")) + sorted(b.INC.glob("*.h")):
         h.update(p.name.encode())
         h.update(p.read_bytes())
-    h.update(" ".join(b.NVFLAGS).encode())
+    h.update(" ".join(f for f in b.NVFLAGS if not f.startswith("/")).encode())  # no machine paths
     return h.hexdigest()
 
 

@@ -63,14 +63,15 @@ static tl_status upload(tl_model* m) {
     const int N = h.N, M = h.M;
     d.nnz_net = (int)h.net_vc.size();
     d.nnz_raw = (int)h.raw_vc.size();
-    // blob: [chan][gkind][net rp][net vc][net cp][net rv] | [raw rp][raw vc]
+    // blob: [chan][ref order][gkind][perm][net rp][net vc][net cp][net rv] | [raw rp][raw vc]
     size_t off = 0;
     auto sect = [&](size_t bytes) {
         const size_t o = off;
         off += al16(bytes);
         return (int)o;
     };
-    d.off_chan = sect((size_t)M * 16);
+    d.off_chan = sect((size_t)M * 8);
+    d.off_rord = sect((size_t)M);
     d.off_gkind = sect((size_t)N);
     d.off_perm = sect((size_t)N * 4);
     d.off_rp = sect((size_t)(N + 1) * 4);
@@ -82,9 +83,11 @@ static tl_status upload(tl_model* m) {
     d.off_raw_vc = sect((size_t)d.nnz_raw * 4);
     d.blob_bytes = off;
     std::vector<unsigned char> hb(off, 0);
-    int4* chan = reinterpret_cast<int4*>(hb.data() + d.off_chan);
+    // channel record: {s0, s1 | order << 28} (species indices < 2^28)
+    int2* chan = reinterpret_cast<int2*>(hb.data() + d.off_chan);
     for (int j = 0; j < M; ++j)
-        chan[j] = make_int4(h.s0[(size_t)j], h.s1[(size_t)j], h.order[(size_t)j], h.ref_order[(size_t)j]);
+        chan[j] = make_int2(h.s0[(size_t)j], h.s1[(size_t)j] | ((int)h.order[(size_t)j] << 28));
+    memcpy(hb.data() + d.off_rord, h.ref_order.data(), (size_t)M);
     memcpy(hb.data() + d.off_gkind, h.gkind.data(), (size_t)N);
     memcpy(hb.data() + d.off_perm, h.rowperm.data(), (size_t)N * 4);
     memcpy(hb.data() + d.off_rp, h.net_rp.data(), (size_t)(N + 1) * 4);
@@ -133,7 +136,8 @@ static MView global_view(const tl_model* m, bool raw_mu, bool raw_update) {
     const DevModel& d = m->d;
     const unsigned char* b = d.blob;
     MView v;
-    v.chan = reinterpret_cast<const int4*>(b + d.off_chan);
+    v.chan = reinterpret_cast<const int2*>(b + d.off_chan);
+    v.rord = reinterpret_cast<const signed char*>(b + d.off_rord);
     v.gkind = reinterpret_cast<const signed char*>(b + d.off_gkind);
     v.perm = reinterpret_cast<const int*>(b + d.off_perm);
     const int* nrp = reinterpret_cast<const int*>(b + d.off_rp);
@@ -286,6 +290,7 @@ static tl_status make_plan(const tl_model* m, int variant, int block_req, int mo
 struct RunBuffers {
     float* rates = nullptr;
     double* tfin = nullptr;
+    double* grid = nullptr;
     int* tracked = nullptr;
     void* samples = nullptr;
     float* scores = nullptr;
@@ -314,8 +319,9 @@ struct Job {
     size_t w = 4;
     std::vector<float> hrates;
     std::vector<double> htf;
+    std::vector<double> hgrid;  // [S][P] grid times
     Plan pl;
-    size_t o_rates = 0, o_tf = 0, o_tr = 0, o_samp = 0, o_sc = 0, o_ctr = 0, o_mean = 0, o_sd = 0, o_grad = 0,
+    size_t o_rates = 0, o_tf = 0, o_grid = 0, o_tr = 0, o_samp = 0, o_sc = 0, o_ctr = 0, o_mean = 0, o_sd = 0, o_grad = 0,
            o_gse = 0, o_gm = 0, o_ps = 0, o_pslot = 0, o_aall = 0, o_gslot = 0;
     RunBuffers rb;
     SimParams p{};
@@ -393,6 +399,13 @@ static tl_status job_prepare(Job& J) {
                 return TL_ERR_INVALID_ARGUMENT;
             }
         }
+    // grid t_k = T*k/n_int (FP64, the last point T itself)
+    J.hgrid.resize((size_t)J.S * J.P);
+    for (int s = 0; s < J.S; ++s)
+        for (int k = 0; k < J.P; ++k)
+            J.hgrid[(size_t)s * J.P + k] = k >= cfg->n_intervals
+                                               ? J.htf[(size_t)s]
+                                               : J.htf[(size_t)s] * (double)k / (double)cfg->n_intervals;
     return ensure_device(m);
 }
 
@@ -400,6 +413,7 @@ static void job_layout(Job& J, Carver& c) {
     const int M = J.m->h.M, N = J.m->h.N, K1 = std::max(J.K, 1);
     J.o_rates = c.take((size_t)J.S * M * 4);
     J.o_tf = c.take((size_t)J.S * 8);
+    J.o_grid = c.take((size_t)J.S * J.P * 8);
     J.o_tr = c.take((size_t)K1 * 4);
     J.o_samp = c.take((size_t)J.total * J.P * K1 * J.w);
     J.o_sc = J.sens ? c.take((size_t)J.total * M * 4) : 0;
@@ -421,6 +435,7 @@ static tl_status job_bind(Job& J, unsigned char* B, cudaStream_t st) {
     RunBuffers& rb = J.rb;
     rb.rates = reinterpret_cast<float*>(B + J.o_rates);
     rb.tfin = reinterpret_cast<double*>(B + J.o_tf);
+    rb.grid = reinterpret_cast<double*>(B + J.o_grid);
     rb.tracked = reinterpret_cast<int*>(B + J.o_tr);
     rb.samples = B + J.o_samp;
     rb.scores = J.sens ? reinterpret_cast<float*>(B + J.o_sc) : nullptr;
@@ -439,6 +454,7 @@ static tl_status job_bind(Job& J, unsigned char* B, cudaStream_t st) {
     }
     TLC(cudaMemcpyAsync(rb.rates, J.hrates.data(), J.hrates.size() * 4, cudaMemcpyHostToDevice, st));
     TLC(cudaMemcpyAsync(rb.tfin, J.htf.data(), J.htf.size() * 8, cudaMemcpyHostToDevice, st));
+    TLC(cudaMemcpyAsync(rb.grid, J.hgrid.data(), J.hgrid.size() * 8, cudaMemcpyHostToDevice, st));
     if (J.K > 0) TLC(cudaMemcpyAsync(rb.tracked, cfg->tracked, (size_t)J.K * 4, cudaMemcpyHostToDevice, st));
     TLC(cudaMemsetAsync(rb.ctr, 0, 64, st));
     SimParams& p = J.p;
@@ -449,6 +465,7 @@ static tl_status job_bind(Job& J, unsigned char* B, cudaStream_t st) {
     p.x0 = m->d.x0;
     p.rates = rb.rates;
     p.t_final = rb.tfin;
+    p.grid = rb.grid;
     p.R = J.R;
     p.r_off = cfg->realization_offset;
     p.S = J.S;
@@ -470,6 +487,7 @@ static tl_status job_bind(Job& J, unsigned char* B, cudaStream_t st) {
     p.blob = m->d.blob;
     p.stage_bytes = J.pl.stage;
     p.off_chan = m->d.off_chan;
+    p.off_rord = m->d.off_rord;
     p.off_gkind = m->d.off_gkind;
     p.off_perm = m->d.off_perm;
     p.off_rp = m->d.off_rp;
@@ -533,12 +551,7 @@ static tl_status job_finish(Job& J, double kernel_ms, int launches, double total
         }
     }
     if (res) {
-        if (res->times)
-            for (int s = 0; s < J.S; ++s)
-                for (int k = 0; k < J.P; ++k)
-                    res->times[(size_t)s * J.P + k] = k == J.cfg->n_intervals
-                                                          ? J.htf[(size_t)s]
-                                                          : J.htf[(size_t)s] * (double)k / (double)J.cfg->n_intervals;
+        if (res->times) std::copy(J.hgrid.begin(), J.hgrid.end(), res->times);
         res->leaps = (int64_t)J.hc[1];
         res->ssa_steps = (int64_t)J.hc[2];
         res->rejections = (int64_t)J.hc[3];

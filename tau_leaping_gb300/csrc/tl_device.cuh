@@ -292,9 +292,9 @@ TL_D int poisson_reference(float mu, Rng& rng) {
 }
 
 // The draw of one channel once its k <= 1 tests have failed (or its mean is
-// >= 10, or the reference's sampler is asked for), out of line: it is the
-// rare path of a leap, and keeping it out of the unrolled channel loop keeps
-// the hot loop small in the instruction cache.
+// >= 10, or the reference's sampler is asked for).  Warp and CTA groups run
+// it from one call site after the unrolled channel loop (pass_fire), so one
+// copy of it sits in the loop.
 // REFS: the reference's sampler can be asked for (compatibility builds).
 template <bool REFS>
 TL_D int poisson_rare_inline(float mu, float q, uint32_t j, uint32_t step, uint32_t r, uint32_t set, uint32_t k0,
@@ -304,15 +304,27 @@ TL_D int poisson_rare_inline(float mu, float q, uint32_t j, uint32_t step, uint3
     if (REFS && refs) return poisson_reference(mu, rng);
     return poisson_tail2(mu, q, rng);
 }
+// Inlined there by default (TL_RARE_INLINE 1): a call would save the
+// registers live across it, and those saves were most of the warp kernel's
+// spills.  Measured on GB300 against the out-of-line call: toy network +3 %,
+// chain +4 %, colloid +1 %, batch +2 %.
+#ifndef TL_RARE_INLINE
+#define TL_RARE_INLINE 1
+#endif
+#if TL_RARE_INLINE
+#define TL_RARE_ATTR __forceinline__
+#else
+#define TL_RARE_ATTR __noinline__
+#endif
 template <bool REFS>
-static __device__ __noinline__ int poisson_rare(float mu, float q, uint32_t j, uint32_t step, uint32_t r,
+static __device__ TL_RARE_ATTR int poisson_rare(float mu, float q, uint32_t j, uint32_t step, uint32_t r,
                                                 uint32_t set, uint32_t k0, uint32_t k1, int refs) {
     return poisson_rare_inline<REFS>(mu, q, j, step, r, set, k0, k1, refs);
 }
 
 // ---------------------------------------------------------------------------
 // Propensity and criticality of one channel (functions.h:100-123).
-// chan = {s0, s1, order, reference order}; order 0 = no reactant (a = c).
+// chan = {s0, s1 | order << 28}; order 0 = no reactant (a = c).
 // ---------------------------------------------------------------------------
 // Population to FP32.  int64 -> float runs at the reduced FP64 rate; an
 // int64 population that fits in int32 (the usual case) takes the 32-bit
@@ -322,15 +334,15 @@ static __device__ __noinline__ float popf_wide(long long x) { return (float)x; }
 TL_D float popf(long long x) { return (long long)(int)x == x ? (float)(int)x : popf_wide(x); }
 
 template <class Pop>
-TL_D void propensity(const int4 ch, float c, const Pop* x, int nc, bool compat_crit, float& a,
+TL_D void propensity(const int2 ch, float c, const Pop* x, int nc, bool compat_crit, float& a,
                      bool& crit) {
     // Branch-free over the order so that a warp's mixed-order channels do
     // not diverge.  For order 1/3 the table holds s1 = s0 (order 0: s0 = s1
     // = 0), so both loads are always in bounds.  The products keep the
     // reference's evaluation order: (c*x0)*x1, and (c*x0)*(x0-1)/2 with the
     // halving exact.
-    const int order = ch.z;
-    const Pop x0 = x[ch.x], x1 = x[ch.y];
+    const int order = (int)((unsigned)ch.y >> 28);
+    const Pop x0 = x[ch.x], x1 = x[ch.y & 0x0FFFFFFF];
     // second factor picked as an integer first: two conversions per channel
     const Pop y = order == 2 ? x1 : order == 3 ? x0 - 1 : (Pop)1;
     const float f0 = order == 0 ? 1.f : popf(x0);
@@ -601,7 +613,8 @@ struct GCta {
 // Model view (global or staged copy in shared memory).
 // ---------------------------------------------------------------------------
 struct MView {
-    const int4* chan;         // [M] {s0, s1, order, reference order}
+    const int2* chan;         // [M] {s0, s1 | order << 28}
+    const signed char* rord;  // [M] the reference's order detector (-1, 1, 2, 3)
     const signed char* gkind; // [N]
     const int* perm;          // [N] row processing order (longest rows first)
     const int* rp;            // [N+1] CSR used for mu/sigma^2
@@ -624,6 +637,7 @@ struct SimParams {
     const void* x0;     // Pop[N]
     const float* rates; // [S][M]
     const double* t_final; // [S]
+    const double* grid;    // [S][n_int+1] grid times
     long long R;        // realizations per set in this call
     long long r_off;    // id of the first realization (sharding)
     int S;
@@ -644,7 +658,7 @@ struct SimParams {
     // staging of the constant blob into shared memory
     const unsigned char* blob;
     int stage_bytes;    // 0 = no staging
-    int off_chan, off_gkind, off_perm, off_rp, off_vc, off_cp, off_rv;  // byte offsets (net)
+    int off_chan, off_rord, off_gkind, off_perm, off_rp, off_vc, off_cp, off_rv;  // byte offsets (net)
     int slot_bytes;     // per group
     int row_warp;       // CTA groups: one warp per species row (long rows)
     unsigned char* gslots;  // CTA groups whose slot exceeds shared memory:
@@ -684,6 +698,10 @@ struct Slot {
                // likelihood-ratio scores, which read a[] after the leap
 };
 
+// Per-realization progress.  Every leap attempt and every direct-method
+// step advances the Philox step counter once, so the counts need no
+// registers of their own: accepted steps nsteps = leaps + ssa, and
+// step = nsteps + rejections.
 template <class TimeT>
 struct RState {
     TimeT t;
@@ -691,7 +709,7 @@ struct RState {
     uint32_t step;     // Philox step counter
     int done;
     long long nsteps;  // accepted steps (cap)
-    long long leaps, ssa, rej;
+    uint32_t ssa;      // direct-method steps
 };
 
 TL_HD bool flag(unsigned f, unsigned b) { return (f & b) != 0; }
@@ -702,10 +720,12 @@ TL_D bool cflag(unsigned f, unsigned b) {
     return COMPAT && (f & b) != 0;
 }
 
+// Grid time k of rate set `set`: T*k/n_int (T itself for k = n_int), from
+// the table the host fills with exactly that FP64 expression, so that a leap
+// loads one double instead of dividing on the reduced-rate FP64 pipe.
 template <class TimeT>
-TL_D TimeT grid_time(const SimParams& p, double T, int k) {
-    if (k >= p.n_int) return (TimeT)T;
-    return (TimeT)(T * (double)k / (double)p.n_int);
+TL_D TimeT grid_time(const SimParams& p, int set, int k) {
+    return (TimeT)__ldg(p.grid + (size_t)set * (p.n_int + 1) + k);
 }
 
 // ---------------------------------------------------------------------------
@@ -739,7 +759,7 @@ TL_D float species_bound(const SimParams& p, const MView& mv, const Pop* x, cons
     const float xi = popf(x[i]);
     float gi;
     if (cg) {
-        const int ord = i < p.M ? mv.chan[i].w : 0;
+        const int ord = i < p.M ? mv.rord[i] : 0;
         gi = (ord >= 1 && ord <= 3) ? (ord == 3 ? 2.f + 1.f / (xi - 1.f) : (float)ord) : 0.f;
     } else {
         gi = g_of(mv.gkind[i], xi);
@@ -962,41 +982,52 @@ TL_D void pass_fire(const Grp& g, const SimParams& p, const float* a, int* kk, f
         }
         U4 gw{0u, 0u, 0u, 0u};
         if (need && !refs) gw = group_words(p.k0, p.k1, (uint32_t)g4, step, r, set);
+        // hot path: criticals, zero means, and the k = 0 / k = 1 tests of
+        // poisson_first on the shared word; the draws that go on (k >= 2,
+        // means >= 10, the reference's sampler) are marked in `rare`
+        // Thread groups (one realization per thread, latency-bound) finish
+        // each long draw in place; warp and CTA groups mark them in `rare`
         int kv[4];
+        unsigned rare = 0;
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
-            const int j = j0 + e;
+            int k = 0;
             if (is_crit(av[e])) {
-                kv[e] = (j == jc) ? 1 : 0;
+                k = (j0 + e == jc) ? 1 : 0;
             } else {
                 const float mu = av[e] * tauf;
-                int k = 0;
-                float q = 0.f;
-                bool rare = refs && mu > 0.f;
-                if (!refs && mu > 0.f) {
-                    // hot path: the k = 0 and k = 1 tests of poisson_first on
-                    // the shared word
-                    q = ((float)word_of(gw, e) + 0.5f) * 2.3283064365386963e-10f;
-                    if (mu >= 10.f) {
-                        rare = true;
-                    } else {
-                        const float s0 = poisson_p1(mu);
-                        if (q < s0) {
-                            if (q >= poisson_p2(mu)) k = 1;
-                            else rare = true;
-                        }
+                if (mu > 0.f) {
+                    bool more = refs || mu >= 10.f;
+                    const float q = refs ? 0.f : ((float)word_of(gw, e) + 0.5f) * 2.3283064365386963e-10f;
+                    if (!more && q < poisson_p1(mu)) {
+                        if (q >= poisson_p2(mu)) k = 1;
+                        else more = true;
+                    }
+                    if (more) {
+                        if constexpr (Grp::kWidth == 1)
+                            k = poisson_rare_inline<COMPAT>(mu, q, (uint32_t)(j0 + e), step, r, set, p.k0, p.k1,
+                                                            refs ? 1 : 0);
+                        else
+                            rare |= 1u << e;
                     }
                 }
-                if (rare) {
-                    // thread groups inline the rare draw (their loop is per
-                    // thread anyway); warp / CTA groups call it out of line
-                    if constexpr (Grp::kWidth == 1)
-                        k = poisson_rare_inline<COMPAT>(mu, q, (uint32_t)j, step, r, set, p.k0, p.k1, refs ? 1 : 0);
-                    else
-                        k = poisson_rare<COMPAT>(mu, q, (uint32_t)j, step, r, set, p.k0, p.k1, refs ? 1 : 0);
-                }
-                kv[e] = k;
             }
+            kv[e] = k;
+        }
+        // the marked draws, from one call site (one copy of the long draw in
+        // the loop rather than one per unrolled channel)
+        while (rare) {
+            const int e = __ffs(rare) - 1;
+            rare &= rare - 1;
+            const float mu = (e == 0 ? av[0] : e == 1 ? av[1] : e == 2 ? av[2] : av[3]) * tauf;
+            const float q = refs ? 0.f : ((float)word_of(gw, e) + 0.5f) * 2.3283064365386963e-10f;
+            const uint32_t j = (uint32_t)(j0 + e);
+            // out of line unless TL_RARE_INLINE
+            const int k = poisson_rare<COMPAT>(mu, q, j, step, r, set, p.k0, p.k1, refs ? 1 : 0);
+            kv[0] = e == 0 ? k : kv[0];
+            kv[1] = e == 1 ? k : kv[1];
+            kv[2] = e == 2 ? k : kv[2];
+            kv[3] = e == 3 ? k : kv[3];
         }
         if (full) {
             *reinterpret_cast<int4*>(kk + j0) = make_int4(kv[0], kv[1], kv[2], kv[3]);
@@ -1058,7 +1089,7 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
             // the waiting time in FP32 (FP64 keeps only the time sum)
             const float ex = -logf(u01f(w.x));
             const TimeT dt = (TimeT)(cflag<COMPAT>(f, TL_FLAG_COMPAT_TAU2) ? ex / fabsf(s.a[j]) : ex / (float)a0);
-            while (st.kpt <= p.n_int && st.t + dt >= grid_time<TimeT>(p, T, st.kpt))
+            while (st.kpt <= p.n_int && st.t + dt >= grid_time<TimeT>(p, set, st.kpt))
                 record_point<Grp, Pop>(g, p, s.x, samp, st.kpt++);
             if (st.kpt > p.n_int) {
                 if (SENS && score) {
@@ -1099,7 +1130,7 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
     }
 
     // ---- tau-leap with negative-population rejection (CGP 2006 steps 3-5) ----
-    const TimeT t_next = grid_time<TimeT>(p, T, st.kpt);
+    const TimeT t_next = grid_time<TimeT>(p, set, st.kpt);
     TimeT t_new;      // time after the leap (unless clamped to t_next)
     float tau_used;   // the leap's tau
     bool clamp;
@@ -1133,10 +1164,9 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
         }
         if (!fire) jc = -1;
         pass_fire<Grp, COMPAT>(g, p, s.a, s.k, tauf, jc, st.step, r, (uint32_t)set);
-        int* kk = s.k;
         g.sync();
         bool ovf = false;
-        const bool bad = pass_update<Grp, Pop>(g, p, mv, s.x, kk, s.xn, ovf);
+        const bool bad = pass_update<Grp, Pop>(g, p, mv, s.x, s.k, s.xn, ovf);
         if (ovf) {
             if (g.leader()) atomicOr((unsigned*)(p.ctr + 5), kErrOverflow);
             st.done = 1;
@@ -1146,7 +1176,6 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
         if (!bad) break;
         // reject: halve tau1, fresh counters, same state
         st.step++;
-        st.rej++;
         tau1 *= 0.5f;
         g.sync();
         pass_props<Grp, Pop, COMPAT>(g, p, mv, rate, s.x, s.a, pa, pac);
@@ -1176,7 +1205,6 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
     }
     st.t = clamp ? t_next : t_new;
     st.step++;
-    st.leaps++;
     st.nsteps++;
     if (clamp) {
         record_point<Grp, Pop>(g, p, s.x, samp, st.kpt);

@@ -66,7 +66,7 @@ struct DevModel {
     unsigned char* blob = nullptr;  // staged constants (net) followed by raw CSR
     size_t blob_bytes = 0;
     int stage_bytes = 0;            // bytes of the net part (what a CTA stages)
-    int off_chan = 0, off_gkind = 0, off_perm = 0, off_rp = 0, off_vc = 0, off_cp = 0, off_rv = 0;
+    int off_chan = 0, off_rord = 0, off_gkind = 0, off_perm = 0, off_rp = 0, off_vc = 0, off_cp = 0, off_rv = 0;
     int off_raw_rp = 0, off_raw_vc = 0;
     void* x0 = nullptr;             // Pop[N]
     float* rate = nullptr;          // [M]

@@ -88,7 +88,8 @@ TL_D bool stage_blob(unsigned char* dst, const unsigned char* src, int bytes, in
 
 TL_D MView staged_view(const unsigned char* s, const SimParams& p) {
     MView v;
-    v.chan = reinterpret_cast<const int4*>(s + p.off_chan);
+    v.chan = reinterpret_cast<const int2*>(s + p.off_chan);
+    v.rord = reinterpret_cast<const signed char*>(s + p.off_rord);
     v.gkind = reinterpret_cast<const signed char*>(s + p.off_gkind);
     v.perm = reinterpret_cast<const int*>(s + p.off_perm);
     v.rp = reinterpret_cast<const int*>(s + p.off_rp);
@@ -149,9 +150,10 @@ struct GroupOf<0> {
 };
 
 // One realization from x0 to t_final (the body of the persistent loop).
+// The realization's step counts go straight to the run's counters (one
+// atomic each per realization), so no totals stay live across the loop.
 template <class Grp, class Pop, bool SENS, bool COMPAT = true>
-TL_D void run_realization(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& s, long long w,
-                          long long& nl, long long& ns, long long& nr, long long& ntr) {
+TL_D void run_realization(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& s, long long w) {
     const int P = p.n_int + 1;
     const int set = (int)(w / p.R);
     const uint32_t r = (uint32_t)(p.r_off + w - (long long)set * p.R);
@@ -162,19 +164,24 @@ TL_D void run_realization(const Grp& g, const SimParams& p, const MView& mv, Slo
     if (SENS && score)
         for (int j = g.rank(); j < p.M; j += g.size()) score[j] = 0.f;
     g.sync();
-    RState<double> st{0.0, 1, 0u, 0, 0, 0, 0, 0};
+    RState<double> st{0.0, 1, 0u, 0, 0, 0u};
     record_point<Grp, Pop>(g, p, s.x, samp, 0);
+    bool trunc = false;
     while (!st.done) {
         do_step<Grp, Pop, double, SENS, COMPAT>(g, p, mv, s, set, r, samp, score, st);
         if (!st.done && p.max_steps > 0 && st.nsteps >= p.max_steps) {
             while (st.kpt <= p.n_int) record_point<Grp, Pop>(g, p, s.x, samp, st.kpt++);
             st.done = 1;
-            ntr++;
+            trunc = true;
         }
     }
-    nl += st.leaps;
-    ns += st.ssa;
-    nr += st.rej;
+    if (g.leader()) {
+        const long long leaps = st.nsteps - (long long)st.ssa, rej = (long long)st.step - st.nsteps;
+        if (leaps) atomicAdd(p.ctr + 1, (unsigned long long)leaps);
+        if (st.ssa) atomicAdd(p.ctr + 2, (unsigned long long)st.ssa);
+        if (rej) atomicAdd(p.ctr + 3, (unsigned long long)rej);
+        if (trunc) atomicAdd(p.ctr + 4, 1ull);
+    }
     g.sync();
 }
 
@@ -229,33 +236,19 @@ __global__ void __launch_bounds__(KIND == 0 ? 1024 : 256, KIND == 0 ? 1 : KIND =
     if constexpr (GSLOT) slots = p.gslots + (size_t)blockIdx.x * (size_t)p.slot_bytes;
     Slot<Pop> s = carve_slot<Pop>(slots + (size_t)GroupOf<KIND>::index() * p.slot_bytes, p);
     const long long total = p.R * (long long)p.S;
-    long long nl = 0, ns = 0, nr = 0, ntr = 0;
 
     for (;;) {
         long long w = 0;
         if (g.leader()) w = (long long)atomicAdd(p.ctr + 0, 1ull);
         w = g.bcast(w, 0);
         if (w >= total) break;
-        run_realization<Grp, Pop, (MODE >= kModeScores), (MODE == kModeGeneral)>(g, p, mv, s, w, nl, ns, nr, ntr);
-    }
-    if (g.leader()) {
-        if (nl) atomicAdd(p.ctr + 1, (unsigned long long)nl);
-        if (ns) atomicAdd(p.ctr + 2, (unsigned long long)ns);
-        if (nr) atomicAdd(p.ctr + 3, (unsigned long long)nr);
-        if (ntr) atomicAdd(p.ctr + 4, (unsigned long long)ntr);
+        run_realization<Grp, Pop, (MODE >= kModeScores), (MODE == kModeGeneral)>(g, p, mv, s, w);
     }
 }
 
 // ---------------------------------------------------------------------------
 // Batched persistent kernel: items of several models / configurations.
 // ---------------------------------------------------------------------------
-TL_D void add_counts(unsigned long long* ctr, long long nl, long long ns, long long nr, long long ntr) {
-    if (nl) atomicAdd(ctr + 1, (unsigned long long)nl);
-    if (ns) atomicAdd(ctr + 2, (unsigned long long)ns);
-    if (nr) atomicAdd(ctr + 3, (unsigned long long)nr);
-    if (ntr) atomicAdd(ctr + 4, (unsigned long long)ntr);
-}
-
 template <class Pop, int MODE>
 __global__ void __launch_bounds__(256, TL_BATCH_MINB) k_batch(BatchParams bp) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -290,21 +283,16 @@ __global__ void __launch_bounds__(256, TL_BATCH_MINB) k_batch(BatchParams bp) {
         const int soff = bp.items[it].stage_off;
         const MView mv = soff >= 0 ? staged_view(smem + soff, p) : p.g;
         const long long local = u - bp.items[it].unit_begin;
-        long long a = 0, b = 0, c = 0, d = 0;
         if (!bp.items[it].lane_mode) {
             const GWarp g{lane};
             Slot<Pop> s = carve_slot<Pop>(wslot, p);
-            run_realization<GWarp, Pop, (MODE >= kModeScores), (MODE == kModeGeneral)>(g, p, mv, s, local, a, b,
-                                                                                      c, d);
-            if (lane == 0) add_counts(p.ctr, a, b, c, d);  // state is replicated across the warp
+            run_realization<GWarp, Pop, (MODE >= kModeScores), (MODE == kModeGeneral)>(g, p, mv, s, local);
         } else {
             const long long wi = local * 32 + lane;
             if (wi < p.R * (long long)p.S) {
                 const G1 g{};
                 Slot<Pop> s = carve_slot<Pop>(wslot + (size_t)lane * p.slot_bytes, p);
-                run_realization<G1, Pop, (MODE >= kModeScores), (MODE == kModeGeneral)>(g, p, mv, s, wi, a, b, c,
-                                                                                     d);
-                add_counts(p.ctr, a, b, c, d);
+                run_realization<G1, Pop, (MODE >= kModeScores), (MODE == kModeGeneral)>(g, p, mv, s, wi);
             }
         }
         __syncwarp();
@@ -369,7 +357,7 @@ __global__ void k_plain_step(SimParams p, float* a_all) {
     const uint32_t r = (uint32_t)(p.r_off + w - (long long)set * p.R);
     const int P = p.n_int + 1;
     Pop* samp = reinterpret_cast<Pop*>(p.samples) + (size_t)w * P * p.K;
-    RState<float> st{q.t, q.kpt, q.step, 0, q.nsteps, 0, 0, 0};
+    RState<float> st{q.t, q.kpt, q.step, 0, q.nsteps, 0u};
     const G1 g{};
     do_step<G1, Pop, float, false>(g, p, p.g, s, set, r, samp, nullptr, st);
     if (!st.done && p.max_steps > 0 && st.nsteps >= p.max_steps) {
@@ -377,13 +365,15 @@ __global__ void k_plain_step(SimParams p, float* a_all) {
         st.done = 1;
         q.trunc++;
     }
+    // this launch's counts from the step counters (see RState)
+    const long long acc = st.nsteps - q.nsteps;
+    q.leaps += acc - (long long)st.ssa;
+    q.ssa += st.ssa;
+    q.rej += (long long)(st.step - q.step) - acc;
     q.t = st.t;
     q.kpt = st.kpt;
     q.step = st.step;
     q.nsteps = st.nsteps;
-    q.leaps += st.leaps;
-    q.ssa += st.ssa;
-    q.rej += st.rej;
     if (s.x != x_before) q.par ^= 1;
     q.done = st.done;
     *ps = q;
