@@ -31,16 +31,14 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_integration_binding_compiles_and_links(tmp_path):
-    """The C++ `Model` class that INTEGRATION.md gives a maintainer of the
-    reference builds against include/tl.h and links against libtl.so."""
+    """The C++ `Model` class a maintainer of the reference adds
+    (tau_leaping_gb300/host/gpu_model.h) builds against include/tl.h and
+    links against libtl.so."""
     import shutil
     import subprocess
     gxx = shutil.which("g++")
     if gxx is None:
         pytest.skip("no g++")
-    text = (ROOT / "INTEGRATION.md").read_text()
-    code = re.search(r"```cpp\n(.*?)```", text, flags=re.S).group(1)
-    (tmp_path / "gpu_model.h").write_text(code)
     (tmp_path / "main.cpp").write_text(
         '#include "gpu_model.h"\n'
         "int main(int argc, char** argv) {\n"
@@ -53,7 +51,8 @@ def test_integration_binding_compiles_and_links(tmp_path):
         "    delete m;\n"
         "}\n")
     lib = ROOT / "tau_leaping_gb300"
-    r = subprocess.run([gxx, "-std=c++17", "-I", str(ROOT / "include"), str(tmp_path / "main.cpp"), "-L", str(lib),
+    r = subprocess.run([gxx, "-std=c++17", "-I", str(ROOT / "include"), "-I", str(lib / "host"),
+                        str(tmp_path / "main.cpp"), "-L", str(lib),
                         "-ltl", f"-Wl,-rpath,{lib}", "-o", str(tmp_path / "a.out")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert subprocess.run([str(tmp_path / "a.out")]).returncode == 0  # no model given: exits before any GPU call
