@@ -998,10 +998,13 @@ TL_D void pass_fire(const Grp& g, const SimParams& p, const float* a, int* kk, f
                 const float mu = av[e] * tauf;
                 if (mu > 0.f) {
                     bool more = refs || mu >= 10.f;
-                    const float q = refs ? 0.f : ((float)word_of(gw, e) + 0.5f) * 2.3283064365386963e-10f;
-                    if (!more && q < poisson_p1(mu)) {
-                        if (q >= poisson_p2(mu)) k = 1;
-                        else more = true;
+                    float q = 0.f;
+                    if (!more) {
+                        q = ((float)word_of(gw, e) + 0.5f) * 2.3283064365386963e-10f;
+                        if (q < poisson_p1(mu)) {
+                            if (q >= poisson_p2(mu)) k = 1;
+                            else more = true;
+                        }
                     }
                     if (more) {
                         if constexpr (Grp::kWidth == 1)

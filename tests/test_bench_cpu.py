@@ -47,3 +47,27 @@ def test_ncu_record_is_used_only_for_the_same_kernel_build(tmp_path, monkeypatch
     (tmp_path / "profiles" / "k_fused_toy.ncu.json").write_text(json.dumps(rec))
     got, why = bench.ncu_record("k_fused_toy")
     assert got is None and "another kernel build" in why
+
+
+def test_reference_arm_runs_the_oracle_only():
+    """`bench.py --impl reference` builds its model with the oracle's own
+    generator and never maps the engine library; its JSON line carries the
+    same config as the engine's arm."""
+    import subprocess
+    code = ("import runpy, sys\n"
+            "sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '3',\n"
+            "            '--realizations', '64', '--t-final', '0.005']\n"
+            "try:\n"
+            "    runpy.run_path('bench.py', run_name='__main__')\n"
+            "finally:\n"
+            "    maps = open('/proc/self/maps').read()\n"
+            "    print('MAPS', 'libtl.so' in maps, 'liboracle.so' in maps)\n")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = r.stdout.strip().splitlines()
+    assert lines[-1] == "MAPS False True", lines[-1]
+    line = json.loads(lines[-2])
+    wl = bench.WORKLOADS["toy"]
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["config"] == bench.workload_config(wl, 64, 0.005, 1)
+    assert line["e2e"]["h2d_bytes_per_step"] == 0
