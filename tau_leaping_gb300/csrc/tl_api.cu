@@ -192,19 +192,34 @@ static int launch_kind(const Plan& pl) { return pl.gslot ? kKindCtaGlobal : pl.k
 //  * a handful of channels: one realization per thread (all lanes busy on
 //    independent realizations); small ensembles use small blocks so that
 //    every SM gets work;
-//  * per-realization state up to 8 KB: one warp per realization, 256-thread
-//    blocks, model tables staged in shared memory;
+//  * per-realization state up to 8 KB: a group of W lanes of a warp per
+//    realization, 256-thread blocks, model tables staged in shared memory.
+//    W is the smallest of 8, 16 and 32 that leaves each lane at most 16
+//    channels and 8 species rows, provided the ensemble fills the GPU's
+//    warp-group slots at least 8 times over (smaller ensembles keep whole
+//    warps, whose realizations finish sooner); scored runs keep whole warps
+//    (the sub-warp kinds have no scores-only build).  Measured on GB300 over
+//    eight model sizes: 32-channel chain 8 lanes 9.8e8 against a warp 4.3e8,
+//    32 x 64 network 8 lanes 9.6e8 against 6.9e8, the 128 x 256 toy network
+//    16 lanes 3.64e8 against 3.50e8, 128-channel chain 16 lanes = warp,
+//    256 x 512 network and the 40-species colloid a warp;
 //  * up to 64 KB: one 128-thread (up to 1024 channels) or 256-thread CTA per
 //    realization, tables through L1/L2 (chain-sized models: 1024 species
 //    and channels);
 //  * larger: one 1024-thread CTA per realization (propensities of ~30k
 //    channels fill most of the 227 KB of shared memory).
-// The choices follow a sweep of every (variant, block, staging) plan on the
-// four benchmark models on GB300.
-static int heuristic_variant(const tl_model* m, size_t sb) {
-    if (m->h.M <= 16 && m->h.N <= 16) return TL_VARIANT_THREAD;
-    if (sb <= 8 * 1024) return TL_VARIANT_WARP;
-    return TL_VARIANT_CTA;
+// The choices follow sweeps of the (variant, block, staging) plans on GB300.
+static int heuristic_variant(const tl_model* m, size_t sb, long long total, int mode, int nsm) {
+    const int M = m->h.M, N = m->h.N;
+    if (M <= 16 && N <= 16) return TL_VARIANT_THREAD;
+    if (sb > 8 * 1024) return TL_VARIANT_CTA;
+    // warp groups: 256-thread CTAs, 5 per SM
+    constexpr long long kWarpGroupsPerSm = 40;
+    if (mode != kModeScores && total >= 8 * kWarpGroupsPerSm * (long long)nsm) {
+        if (M <= 16 * 8 && N <= 8 * 8) return TL_VARIANT_LANES8;
+        if (M <= 16 * 16 && N <= 8 * 16) return TL_VARIANT_LANES16;
+    }
+    return TL_VARIANT_WARP;
 }
 
 static tl_status make_plan(const tl_model* m, int variant, int block_req, int mode, bool compat_stoich,
@@ -213,10 +228,10 @@ static tl_status make_plan(const tl_model* m, int variant, int block_req, int mo
     const int smax = max_smem_optin() - 2048;
     const int stage = (compat_stoich || no_stage) ? 0 : m->d.stage_bytes;
     const bool autov = variant == TL_VARIANT_AUTO;
-    if (autov) variant = heuristic_variant(m, sb);
+    const int nsm = sm_count();
+    if (autov) variant = heuristic_variant(m, sb, total, mode, nsm);
     pl.variant = variant;
     int groups_per_block = 1;
-    const int nsm = sm_count();
     if (variant == TL_VARIANT_THREAD) {
         pl.kind = 1;
         int b = block_req;
