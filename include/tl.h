@@ -155,9 +155,9 @@ enum tl_variant {
     TL_VARIANT_PLAIN = 4,  /* FP32, one realization per thread, one launch
                               per step: the unfused baseline form           */
     TL_VARIANT_LANES2 = 5,  /* fused persistent, one realization per 2, 4,  */
-    TL_VARIANT_LANES4 = 6,  /* 8 or 16 lanes of a warp (small models on     */
-    TL_VARIANT_LANES8 = 7,  /* ensembles too small to fill the GPU one       */
-    TL_VARIANT_LANES16 = 8  /* realization per thread)                       */
+    TL_VARIANT_LANES4 = 6,  /* 8 or 16 lanes of a warp; AUTO takes 8 or 16  */
+    TL_VARIANT_LANES8 = 7,  /* for models up to 128 or 256 channels on      */
+    TL_VARIANT_LANES16 = 8  /* ensembles that fill the GPU many times over   */
 };
 
 /* Behaviour flags. */

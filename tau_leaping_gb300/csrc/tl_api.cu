@@ -486,6 +486,7 @@ static tl_status job_bind(Job& J, unsigned char* B, cudaStream_t st) {
     p.S = J.S;
     p.k0 = (uint32_t)(cfg->seed & 0xFFFFFFFFu);
     p.k1 = (uint32_t)(cfg->seed >> 32);
+    round_keys(p.k0, p.k1, p.rk);
     p.eps = (float)cfg->eps;
     p.nc = cfg->n_critical > 0 ? cfg->n_critical : 5;
     p.ssa_factor = (float)(cfg->ssa_factor > 0 ? cfg->ssa_factor : 10);

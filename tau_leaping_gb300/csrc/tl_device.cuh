@@ -72,6 +72,27 @@ TL_HD U4 philox10(U4 c, uint32_t k0, uint32_t k1) {
     return c;
 }
 
+// The same Philox4x32-10 with the ten rounds' keys precomputed:
+// rk[2r] = k0 + r*0x9E3779B9, rk[2r+1] = k1 + r*0xBB67AE85.  The engine's
+// kernels read rk from their launch parameters (constant bank), so the key
+// schedule costs no instruction; the words are those of philox10.
+TL_HD U4 philox10rk(U4 c, const uint32_t* rk) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t hi0 = mulhi32(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        const uint32_t hi1 = mulhi32(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        c = U4{hi1 ^ c.y ^ rk[2 * r], lo1, hi0 ^ c.w ^ rk[2 * r + 1], lo0};
+    }
+    return c;
+}
+
+TL_HD void round_keys(uint32_t k0, uint32_t k1, uint32_t* rk) {
+    for (int r = 0; r < 10; ++r) {
+        rk[2 * r] = k0 + (uint32_t)r * 0x9E3779B9u;
+        rk[2 * r + 1] = k1 + (uint32_t)r * 0xBB67AE85u;
+    }
+}
+
 // Uniform in (0,1): 23 random bits at odd multiples of 2^-24 (exact in FP32).
 TL_HD float u01f(uint32_t w) { return ((float)(w >> 9) + 0.5f) * 1.1920928955078125e-07f; }
 // Uniform in (0,1) with 52 random bits, exact in FP64.
@@ -81,27 +102,27 @@ TL_HD double u01d(uint32_t hi, uint32_t lo) {
 }
 
 // Step scalars of (realization r, set s, step): 4 words.
-TL_HD U4 step_words(uint32_t k0, uint32_t k1, uint32_t step, uint32_t r, uint32_t set) {
-    return philox10(U4{kScalarChannel, step, r, set << 8}, k0, k1);
+TL_HD U4 step_words(const uint32_t* rk, uint32_t step, uint32_t r, uint32_t set) {
+    return philox10rk(U4{kScalarChannel, step, r, set << 8}, rk);
 }
 
 // Per-channel uniform stream: blocks (j, step, r, set<<8 | b), b = 0, 1, ...
 struct ChanRng {
     U4 buf;
-    uint32_t j, step, r, c3, k0, k1;
+    uint32_t j, step, r, c3;
+    const uint32_t* rk;  // round keys (philox10rk)
     int left;
-    TL_D void init(uint32_t j_, uint32_t step_, uint32_t r_, uint32_t set, uint32_t k0_, uint32_t k1_) {
+    TL_D void init(uint32_t j_, uint32_t step_, uint32_t r_, uint32_t set, const uint32_t* rk_) {
         j = j_;
         step = step_;
         r = r_;
         c3 = set << 8;
-        k0 = k0_;
-        k1 = k1_;
+        rk = rk_;
         left = 0;
     }
     TL_D float next() {
         if (left == 0) {
-            buf = philox10(U4{j, step, r, c3}, k0, k1);
+            buf = philox10rk(U4{j, step, r, c3}, rk);
             c3 += 1;  // next block; 256 blocks per (j, step) before wrapping into set+1
             left = 4;
         }
@@ -206,8 +227,8 @@ TL_D int poisson_cgp(float mu, Rng& rng) {
 // Shared first words: channels 4g..4g+3 of one step take their first 32-bit
 // word from one Philox block (g, step, r, set<<8 | 0xFF); the private
 // stream (j, step, r, set<<8 | b), b < 0xFF, supplies any further uniforms.
-TL_HD U4 group_words(uint32_t k0, uint32_t k1, uint32_t g, uint32_t step, uint32_t r, uint32_t set) {
-    return philox10(U4{g, step, r, (set << 8) | 0xFFu}, k0, k1);
+TL_HD U4 group_words(const uint32_t* rk, uint32_t g, uint32_t step, uint32_t r, uint32_t set) {
+    return philox10rk(U4{g, step, r, (set << 8) | 0xFFu}, rk);
 }
 
 // P(K >= 1) = 1 - exp(-mu) for 0 < mu: below 0.1 the Taylor series to
@@ -297,10 +318,10 @@ TL_D int poisson_reference(float mu, Rng& rng) {
 // copy of it sits in the loop.
 // REFS: the reference's sampler can be asked for (compatibility builds).
 template <bool REFS>
-TL_D int poisson_rare_inline(float mu, float q, uint32_t j, uint32_t step, uint32_t r, uint32_t set, uint32_t k0,
-                             uint32_t k1, int refs) {
+TL_D int poisson_rare_inline(float mu, float q, uint32_t j, uint32_t step, uint32_t r, uint32_t set,
+                             const uint32_t* rk, int refs) {
     ChanRng rng;
-    rng.init(j, step, r, set, k0, k1);
+    rng.init(j, step, r, set, rk);
     if (REFS && refs) return poisson_reference(mu, rng);
     return poisson_tail2(mu, q, rng);
 }
@@ -318,8 +339,8 @@ TL_D int poisson_rare_inline(float mu, float q, uint32_t j, uint32_t step, uint3
 #endif
 template <bool REFS>
 static __device__ TL_RARE_ATTR int poisson_rare(float mu, float q, uint32_t j, uint32_t step, uint32_t r,
-                                                uint32_t set, uint32_t k0, uint32_t k1, int refs) {
-    return poisson_rare_inline<REFS>(mu, q, j, step, r, set, k0, k1, refs);
+                                                uint32_t set, const uint32_t* rk, int refs) {
+    return poisson_rare_inline<REFS>(mu, q, j, step, r, set, rk, refs);
 }
 
 // ---------------------------------------------------------------------------
@@ -642,6 +663,7 @@ struct SimParams {
     long long r_off;    // id of the first realization (sharding)
     int S;
     uint32_t k0, k1;    // Philox key (seed)
+    uint32_t rk[20];    // its round keys (round_keys)
     float eps;
     int nc;
     float ssa_factor;
@@ -981,7 +1003,7 @@ TL_D void pass_fire(const Grp& g, const SimParams& p, const float* a, int* kk, f
             need |= !is_crit(av[e]) && m > 0.f && m < 10.f;
         }
         U4 gw{0u, 0u, 0u, 0u};
-        if (need && !refs) gw = group_words(p.k0, p.k1, (uint32_t)g4, step, r, set);
+        if (need && !refs) gw = group_words(p.rk, (uint32_t)g4, step, r, set);
         // hot path: criticals, zero means, and the k = 0 / k = 1 tests of
         // poisson_first on the shared word; the draws that go on (k >= 2,
         // means >= 10, the reference's sampler) are marked in `rare`
@@ -1008,7 +1030,7 @@ TL_D void pass_fire(const Grp& g, const SimParams& p, const float* a, int* kk, f
                     }
                     if (more) {
                         if constexpr (Grp::kWidth == 1)
-                            k = poisson_rare_inline<COMPAT>(mu, q, (uint32_t)(j0 + e), step, r, set, p.k0, p.k1,
+                            k = poisson_rare_inline<COMPAT>(mu, q, (uint32_t)(j0 + e), step, r, set, p.rk,
                                                             refs ? 1 : 0);
                         else
                             rare |= 1u << e;
@@ -1026,7 +1048,7 @@ TL_D void pass_fire(const Grp& g, const SimParams& p, const float* a, int* kk, f
             const float q = refs ? 0.f : ((float)word_of(gw, e) + 0.5f) * 2.3283064365386963e-10f;
             const uint32_t j = (uint32_t)(j0 + e);
             // out of line unless TL_RARE_INLINE
-            const int k = poisson_rare<COMPAT>(mu, q, j, step, r, set, p.k0, p.k1, refs ? 1 : 0);
+            const int k = poisson_rare<COMPAT>(mu, q, j, step, r, set, p.rk, refs ? 1 : 0);
             kv[0] = e == 0 ? k : kv[0];
             kv[1] = e == 1 ? k : kv[1];
             kv[2] = e == 2 ? k : kv[2];
@@ -1086,7 +1108,7 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
                     return;
                 }
             }
-            const U4 w = step_words(p.k0, p.k1, st.step, r, (uint32_t)set);
+            const U4 w = step_words(p.rk, st.step, r, (uint32_t)set);
             const TimeT target = (TimeT)u01d(w.z, w.w) * a0;
             const int j = select_channel<Grp, TimeT>(g, p, s.a, pa, target, 0);
             // the waiting time in FP32 (FP64 keeps only the time sum)
@@ -1140,7 +1162,7 @@ TL_D void do_step(const Grp& g, const SimParams& p, const MView& mv, Slot<Pop>& 
     for (int attempt = 0;; ++attempt) {
         const float a0cf = g.sumf(pac);
         // the step's scalar words are needed only when a channel is critical
-        const U4 w = a0cf > 0.f ? step_words(p.k0, p.k1, st.step, r, (uint32_t)set) : U4{0u, 0u, 0u, 0u};
+        const U4 w = a0cf > 0.f ? step_words(p.rk, st.step, r, (uint32_t)set) : U4{0u, 0u, 0u, 0u};
         int jc = -1;
         float tau2 = kInfF;
         if (a0cf > 0.f) {

@@ -216,7 +216,7 @@ TL_D void run_realization(const Grp& g, const SimParams& p, const MView& mv, Slo
 // that the shared-memory kernels keep shared-memory addressing.
 template <int KIND, class Pop, int MODE, bool GSLOT = false>
 __global__ void __launch_bounds__(KIND == 0 ? 1024 : 256, KIND == 0 ? 1 : KIND == 1 ? TL_THREAD_MINB : TL_WARP_MINB)
-    k_fused(SimParams p) {
+    k_fused(const __grid_constant__ SimParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ __align__(8) unsigned long long mbar;
     __shared__ double red[34];
@@ -319,7 +319,7 @@ struct PlainState {
 };
 
 template <class Pop>
-__global__ void k_plain_init(SimParams p) {
+__global__ void k_plain_init(const __grid_constant__ SimParams p) {
     const long long total = p.R * (long long)p.S;
     const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= total) return;
@@ -336,7 +336,7 @@ __global__ void k_plain_init(SimParams p) {
 }
 
 template <class Pop>
-__global__ void k_plain_step(SimParams p, float* a_all) {
+__global__ void k_plain_step(const __grid_constant__ SimParams p, float* a_all) {
     const long long total = p.R * (long long)p.S;
     const long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= total) return;
@@ -545,13 +545,15 @@ __global__ void k_philox(const uint4* ctr, const uint2* key, int n, uint4* out) 
 __global__ void k_poisson(const float* mean, int n, uint32_t k0, uint32_t k1, uint32_t step, int compat, int* out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    uint32_t rk[20];
+    round_keys(k0, k1, rk);
     ChanRng rng;
-    rng.init((uint32_t)i, step, 0u, 0u, k0, k1);
+    rng.init((uint32_t)i, step, 0u, 0u, rk);
     if (compat) {
         out[i] = poisson_reference(mean[i], rng);
     } else {
         // exactly the hot path's draw for channel i of realization 0, set 0
-        const U4 gw = group_words(k0, k1, (uint32_t)i >> 2, step, 0u, 0u);
+        const U4 gw = group_words(rk, (uint32_t)i >> 2, step, 0u, 0u);
         out[i] = poisson_first(mean[i], word_of(gw, i & 3), rng);
     }
 }
