@@ -305,3 +305,23 @@ def test_chain_1024_full_config_error_vs_exact_solution(capsys):
     # method accuracy: sanity bounds against the exact solution
     assert rel_m.max() < 0.02
     assert np.sqrt((rel_v ** 2).mean()) < 0.15
+
+
+def test_heuristic_group_width_follows_model_and_ensemble():
+    """The heuristic's group width (the fewest lanes of 8, 16 and 32 with at
+    most 16 channels and 8 species rows per lane, on ensembles that fill
+    the warp-group slots at least 8 times, unscored runs only), and the
+    16-lane plan of the 128 x 256 network against the FP64 oracle."""
+    toy = Model.generate("toy")
+    big = toy.simulate(0.0005, 100_000, seed=3, tracked=[0, 4])
+    assert big.variant == _ffi.VARIANT_LANES16
+    assert toy.simulate(0.0005, 20_000, seed=3, tracked=[0, 4]).variant == _ffi.VARIANT_WARP
+    assert toy.sensitivity(0.0005, 100_000, seed=3, tracked=[0])["variant"] == _ffi.VARIANT_WARP
+    small = Model.generate("toy", n_species=32, n_channels=64, seed=4, x0_max=3000)
+    assert small.simulate(0.0005, 100_000, seed=3, tracked=[0]).variant == _ffi.VARIANT_LANES8
+    wide = Model.generate("toy", n_species=256, n_channels=512, seed=5)
+    assert wide.simulate(0.0002, 100_000, seed=3, tracked=[0]).variant == _ffi.VARIANT_WARP
+    g = toy.simulate(0.002, 100_000, seed=6, tracked=[0, 4], keep_samples=True)
+    assert g.variant == _ffi.VARIANT_LANES16
+    r = ora.OracleModel.from_desc(toy.desc()).simulate(0.002, 4000, seed=7, tracked=[0, 4], threads=16)
+    compare_final(g.samples[0, :, -1, :], r["samples"][0, :, -1, :], "toy network, 16-lane plan")
