@@ -133,10 +133,11 @@ tl_status derive_tables(HostModel& h, std::string& err) {
     h.s0.assign((size_t)M, 0);
     h.s1.assign((size_t)M, 0);
     h.max_order = 0;
+    std::vector<std::pair<int, int>> re;  // reused: no allocation per channel
     for (int j = 0; j < M; ++j) {
         // the reference's detector (CSCMatrix.cu:204-231)
         int first = 0, second = 0;
-        std::vector<std::pair<int, int>> re;
+        re.clear();
         for (int q = h.col_ptr[(size_t)j]; q < h.col_ptr[(size_t)j + 1]; ++q) {
             const int v = h.stoich[(size_t)q];
             if (v >= 0) continue;
@@ -197,18 +198,34 @@ tl_status derive_tables(HostModel& h, std::string& err) {
     h.net_cp.assign((size_t)M + 1, 0);
     std::vector<int32_t> nrows;
     std::vector<int> nvals;
+    nrows.reserve((size_t)nnz);
+    nvals.reserve((size_t)nnz);
+    std::vector<std::pair<int, int>> col;  // one column's (species, v), reused
     for (int j = 0; j < M; ++j) {
-        std::map<int, int> acc;
-        for (int q = h.col_ptr[(size_t)j]; q < h.col_ptr[(size_t)j + 1]; ++q)
-            acc[h.row_ind[(size_t)q]] += h.stoich[(size_t)q];
-        for (auto& e : acc) {
-            if (e.second == 0) continue;
-            if (!packable(e.second)) {
+        // the column's entries by species (columns hold a handful of
+        // entries: insertion sort), duplicates summed, zeros dropped
+        col.clear();
+        for (int q = h.col_ptr[(size_t)j]; q < h.col_ptr[(size_t)j + 1]; ++q) {
+            std::pair<int, int> e{h.row_ind[(size_t)q], (int)h.stoich[(size_t)q]};
+            size_t k = col.size();
+            col.push_back(e);
+            while (k > 0 && col[k - 1].first > e.first) {
+                col[k] = col[k - 1];
+                --k;
+            }
+            col[k] = e;
+        }
+        for (size_t a = 0; a < col.size();) {
+            const int sp = col[a].first;
+            int v = 0;
+            for (; a < col.size() && col[a].first == sp; ++a) v += col[a].second;
+            if (v == 0) continue;
+            if (!packable(v)) {
                 err = "net stoichiometry outside [-2, 5] cannot be packed";
                 return TL_ERR_UNSUPPORTED;
             }
-            nrows.push_back(e.first);
-            nvals.push_back(e.second);
+            nrows.push_back(sp);
+            nvals.push_back(v);
         }
         h.net_cp[(size_t)j + 1] = (int32_t)nrows.size();
     }
