@@ -10,6 +10,9 @@ take, each driven on purpose and checked through the C ABI:
   5); the engine and the FP64 oracle, which draws the same streams, agree
   trajectory for trajectory, and an independent oracle ensemble agrees at
   99 % (Welch t, Levene, Kolmogorov-Smirnov) with many rejections;
+* small Poisson means on every group kind: the k = 0 / k = 1 tests on the
+  shared Philox word, placed differently per group kind, give the oracle's
+  firing counts trajectory for trajectory;
 * the halving cap: a leap still rejected after max_halvings halvings stops
   its realization and the call returns TL_ERR_NUMERIC;
 * the bounded staging wait: with no polls allowed the wait for the model
